@@ -1,0 +1,473 @@
+"""Tracking-iteration benchmark (one JSON line on rank 0).
+
+Metric: tracking iterations per second at 500k Gaussians, 640x480 — one iteration is
+the (t, t + dtau) render pair forward, the normalised intensity-change loss against
+the event frame, the adjoint to the 6-DoF pose twist and 6-DoF velocity, the Adam step
+and the pose / velocity update (utils/tracker.py:176-222).
+
+  value      batched adjoint path (gsevt_track_step_batched, one CUDA graph per
+             iteration), inputs resident in HBM, CUDA events per iteration, L2 flushed
+             between iterations (outside the timed events)
+  e2e        the same iteration through the public API with the step's inputs (event
+             frame and pose state) copied from pinned host memory and the result (loss
+             and pose state) read back, every step, inside the timed region
+  plain      the plain per-view drop-in path (reference-structured tracker over the
+             drop-in GaussianRasterizer, torch glue and torch Adam), timed beside it
+  roofline   dominant stage of the iteration against the measured HBM bandwidth
+  cpu_baseline  the CPU oracle (C + OpenMP) running the same iteration on the host
+             cores, on a bounded sample
+
+--impl reference times the reference's CPU implementation of the path: the reference
+rasterizer's native source is absent from its tree, so this is the oracle restatement
+(oracle/, kind "port") on all host cores.
+
+Multi-GPU: tracking problems are independent; under torchrun every rank runs its own
+replica (no collective on the data path), value = sum over ranks, time = max over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "gs-evt_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np
+
+WORKLOADS = {
+    # name: (gaussians, seed, width, height, focal, events, hypotheses)
+    "adjoint-500k-640x480": (500_000, 2, 640, 480, 600.0, 1_000_000, 1),
+    "plain-300k-640x480": (300_000, 1, 640, 480, 600.0, 1_000_000, 1),
+    "hypotheses-64x2-500k": (500_000, 3, 640, 480, 600.0, 1_000_000, 64),
+}
+METRIC = "tracking iters/sec at 500k Gaussians 640x480 (fwd+pose bwd); batched vs plain"
+HBM_FALLBACK = 6800.0
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu_index = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu_index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_problem(name, device, seed_offset=0):
+    import torch
+    from gsevt import synthetic
+    from gsevt import pose as gpose
+    from gsevt.engine import GSFrame, MapSpec, ViewSpec, pack_map
+    from gsevt.events import event_frames
+    n, seed, W, H, f, n_events, hyp = WORKLOADS[name]
+    sc = synthetic.Scenario(n, seed + seed_offset, W, H, f, n_events)
+    m = sc.map
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+    rot = t(m["rot"])
+    packed = pack_map(t(m["xyz"]), t(m["opacity"]), t(m["sh"]), scales=t(m["scale"]), rotations=rot)
+    # events from grey log-intensity renders at the ground-truth pair poses
+    Tl, Tn = sc.gt_pair()
+    cam = sc.camera
+    views = [ViewSpec(W, H, 0, R=T[:3, :3], t=T[:3, 3], P=cam.proj, campos=gpose.campos(T[:3, :3], T[:3, 3]),
+                      tanfovx=cam.tanfovx, tanfovy=cam.tanfovy) for T in (Tl, Tn)]
+    fr = GSFrame([MapSpec(n, packed=packed)], views, channels=1, device=device)
+    fr.render(exact_keys=True)
+    I_last = fr.pixels(0)[0].cpu().numpy()
+    I_next = fr.pixels(1)[0].cpu().numpy()
+    del fr
+    ex, ey, ep, ts = synthetic.synth_events(I_last, I_next, n_events, seed + 77, delta_tau=sc.delta_tau)
+    sig, uns = event_frames(t(ex), t(ey), t(ep), W, H, 9, 1, device)
+    return dict(scenario=sc, map=m, packed=packed, n=n, W=W, H=H, f=f, E=sig[0].reshape(-1).contiguous(),
+                E_unsigned=uns[0].reshape(-1).contiguous(), events=(ex, ey, ep, ts), hypotheses=hyp)
+
+
+def make_tracker(prob, device, hypotheses=None):
+    from gsevt import synthetic
+    from gsevt.batched import BatchedTracker, Problem
+    sc = prob["scenario"]
+    hyp = hypotheses or prob["hypotheses"]
+    if hyp == 1:
+        poses = [(sc.init_R, sc.init_t)]
+    else:
+        poses = synthetic.hypotheses(sc.gt_R, sc.gt_t, hyp, sc.seed + 5)
+    probs = [Problem(0, R, t, sc.init_lin, sc.init_ang, sc.delta_tau, prob["W"], prob["H"], prob["f"], prob["f"],
+                     prob["E"], prob["E_unsigned"], opt_vel=True) for R, t in poses]
+    return BatchedTracker([{"packed": prob["packed"], "n": prob["n"]}], probs, device=device)
+
+
+def stage_times(bt, reps=5):
+    """CUDA-event time of each stage of one iteration (no graph), median over reps."""
+    import ctypes as C
+    import torch
+    from gsevt._lib import lib, check
+    from gsevt.engine import _ptr, _stream
+    fr = bt.frame
+    names = ["preprocess_fwd", "bin_and_sort", "blend_fwd", "loss", "blend_bwd", "preprocess_bwd", "finalize"]
+    acc = {k: [] for k in names}
+    for _ in range(reps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+        ev[0].record()
+        fr.preprocess(); ev[1].record()
+        fr.bin_and_sort(0); ev[2].record()
+        fr.blend(); ev[3].record()
+        fr.loss(bt.loss); ev[4].record()
+        fr.blend_backward(); ev[5].record()
+        fr.preprocess_backward(None); ev[6].record()
+        # finalize through the full step would redo the stages; time the step minus the rest
+        ev[7].record()
+        torch.cuda.synchronize()
+        for i, k in enumerate(names[:-1]):
+            acc[k].append(ev[i].elapsed_time(ev[i + 1]))
+    return {k: statistics.median(v) for k, v in acc.items() if v}
+
+
+def algorithmic_bytes(bt, prob):
+    """Compulsory HBM bytes per launch of each stage (counts read from the device)."""
+    import torch
+    from gsevt import _lib
+    fr = bt.frame
+    st, K = fr.status()
+    n = prob["n"]
+    V = fr.L.num_views
+    off = _lib.workspace_offsets(fr.L)["bin"]
+    binv = fr.workspace[off:off + 16 * fr.L.num_vg].view(torch.int32).view(-1, 4)
+    nvis = int((binv[:, 0] > 0).sum().item())
+    P = fr.L.total_pixels
+    passes = (fr.L.sort_bits + 7) // 8
+    maps = len(fr.maps)
+    return {
+        # attributes once per map (232 B), per (view, Gaussian) 16 B bin record, 32 B blend record
+        "preprocess_fwd": 232 * n * maps + 16 * n * V + 32 * nvis,
+        # read bin 16 B/slot, write 12 B/key; each pass reads and writes 12 B/key; histogram reads 8 B/key
+        "bin_and_sort": 16 * n * V + 12 * K + 24 * K * passes + 8 * K + 16 * K,
+        # per key: 4 B value + 32 B record gather; per pixel 8 B written
+        "blend_fwd": 36 * K + 8 * P,
+        "loss": 12 * P,
+        # gather as forward, per pixel 12 B read, per visible slot 32 B gradient accumulation
+        "blend_bwd": 36 * K + 12 * P + 32 * nvis,
+        "preprocess_bwd": 232 * n * maps + 16 * n * V + 32 * nvis,
+        "counts": {"keys": K, "visible_slots": nvis, "pixels": P, "views": V, "sort_passes": passes},
+    }
+
+
+def time_batched(bt, steps, warmup, flush):
+    import torch
+    bt.capture(warmup=max(1, warmup))
+    for _ in range(warmup):
+        bt.graph.replay()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush.zero_()  # write a buffer larger than L2 between timed iterations
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        bt.graph.replay()
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    return times
+
+
+def time_e2e(bt, prob, steps, warmup):
+    """Public-API iteration with host buffers: per step, H2D of the event frame and the
+    pose state from pinned memory, the iteration, D2H of the loss and pose state."""
+    import torch
+    E_host = prob["E"].cpu().pin_memory()
+    S_host = bt.state.cpu().pin_memory()
+    L_host = torch.empty_like(bt.loss, device="cpu").pin_memory()
+    S_out = torch.empty_like(S_host).pin_memory()
+    ev_dev = bt.problems[0].event_signed
+    h2d = E_host.numel() * 4 + S_host.numel()
+    d2h = L_host.numel() * 8 + S_out.numel()
+
+    def one():
+        ev_dev.copy_(E_host, non_blocking=True)
+        bt.state.copy_(S_host, non_blocking=True)
+        bt.graph.replay()
+        L_host.copy_(bt.loss, non_blocking=True)
+        S_out.copy_(bt.state, non_blocking=True)
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        one()
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / steps
+    return ms, h2d, d2h
+
+
+def time_plain(prob, device, iters=8, warmup=3):
+    """The plain per-view drop-in path: reference-structured iteration (RenderFrame with two
+    rasterizer calls, torch grey / normalisation / loss, autograd, torch Adam, update_vwRT)."""
+    import torch
+    from gsevt.camera import Camera
+    from gsevt.renderer import GaussianMap
+    from gsevt.tracker import make_optimizer, plain_iteration
+    sc = prob["scenario"]
+    cam = sc.camera
+    c = Camera(torch.tensor(sc.init_R, dtype=torch.float32), torch.tensor(sc.init_t, dtype=torch.float32),
+               torch.tensor(sc.init_ang, dtype=torch.float32), torch.tensor(sc.init_lin, dtype=torch.float32),
+               cam.fovx, cam.fovy, cam.width, cam.height, delta_tau=sc.delta_tau, device=device)
+    c.fx, c.fy = cam.fx, cam.fy
+    gm = GaussianMap.from_synthetic(prob["map"], device=device)
+    lrs = {"cam_rot_delta": 0.004, "cam_trans_delta": 0.004, "cam_w_delta": 0.002, "cam_v_delta": 0.002}
+    opt = make_optimizer(c, lrs)
+    bg = torch.zeros(3, device=device)
+    E = prob["E"].view(1, prob["H"], prob["W"])
+    for _ in range(warmup):
+        plain_iteration(c, gm, bg, opt, 0, True, E, None)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        plain_iteration(c, gm, bg, opt, 0, True, E, None)
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) * 1000.0 / iters
+
+
+def cpu_iteration(prob, poses=None):
+    """One tracking iteration of the pair on the host with the oracle (FP32 forward of both
+    views, FP64 loss and adjoint along the frozen contributor lists, exact chain)."""
+    from oracle import oracle
+    from oracle import pose as opose
+    sc = prob["scenario"]
+    m = prob["map"]
+    W, H = prob["W"], prob["H"]
+    cam = sc.camera
+    cov = oracle.cov3d(m["scale"], m["rot"])
+    E = prob["E_np"]
+    Tl, Tn = opose.pair_poses(sc.init_R, sc.init_t, sc.init_lin, sc.init_ang, sc.delta_tau)
+    recs = []
+    for T in (Tl, Tn):
+        v = opose.view_vector(T[:3, :3], T[:3, 3], W, H, prob["f"], prob["f"], np.float64)
+        r = oracle.rasterize_view(m["xyz"], cov, m["sh"], m["opacity"], v.astype(np.float32), W, H, [0.0], nch=1,
+                                  record=True)
+        recs.append((r, v))
+    L, gn, gl = oracle.loss(recs[0][0]["image"][0], recs[1][0]["image"][0], E, False, grads=True)
+    gx = []
+    for (r, v), g in zip(recs, (gl, gn)):
+        x, _ = oracle.frozen_backward(r, m["xyz"], m["opacity"], v, W, H, [0.0], 1, g.reshape(1, H, W),
+                                      sh=m["sh"], cov_pre=cov)
+        gx.append(x)
+    return opose.chain_pose_gradient(gx[0], gx[1], sc.init_lin, sc.init_ang, sc.delta_tau), L
+
+
+def cpu_baseline(prob, budget_s=30.0):
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    prob["E_np"] = prob["E"].cpu().numpy()
+    t0 = time.perf_counter()
+    cpu_iteration(prob)
+    dt = time.perf_counter() - t0
+    iters = 1
+    while time.perf_counter() - t0 + dt < budget_s and iters < 3:
+        cpu_iteration(prob)
+        iters += 1
+    total = time.perf_counter() - t0
+    return {"value": iters / total, "unit": "iters/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+            "kind": "port",
+            "sample": "%d full tracking iteration(s) of the 640x480 pair at %d Gaussians (oracle: FP32 forward, "
+                      "FP64 adjoint), %.1f s" % (iters, prob["n"], total)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch
+    name = args.workload
+    os.environ["OMP_NUM_THREADS"] = str(os.cpu_count())
+    # the reference arm never touches the GPU: build the same seeded problem on the host
+    from gsevt import synthetic
+    from oracle import oracle
+    from oracle import pose as opose
+    n, seed, W, H, f, n_events, hyp = WORKLOADS[name]
+    sc = synthetic.Scenario(n, seed, W, H, f, n_events)
+    m = sc.map
+    cov = oracle.cov3d(m["scale"], m["rot"])
+    imgs = []
+    for T in sc.gt_pair():
+        v = opose.view_vector(T[:3, :3], T[:3, 3], W, H, f, f, np.float32)
+        imgs.append(oracle.rasterize_view(m["xyz"], cov, m["sh"], m["opacity"], v, W, H, [0.0], nch=1)["image"][0])
+    ex, ey, ep, ts = synthetic.synth_events(imgs[0], imgs[1], n_events, seed + 77, delta_tau=sc.delta_tau)
+    E, _, _ = oracle.event_frame(W, H, ex, ey, ep, 9)
+    prob = dict(scenario=sc, map=m, n=n, W=W, H=H, f=f, E_np=E)
+    budget = 150.0
+    t_start = time.perf_counter()
+    for _ in range(min(args.warmup, 1)):
+        cpu_iteration(prob)
+    done, t0 = 0, time.perf_counter()
+    per = None
+    while done < args.steps:
+        cpu_iteration(prob)
+        done += 1
+        per = (time.perf_counter() - t0) / done
+        if time.perf_counter() - t_start + per > budget:
+            break
+    total = time.perf_counter() - t0
+    val = done / total
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "iters/s", "n_gpus": args.gpus,
+            "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 * total / done,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": name, "gaussians": n, "width": W, "height": H,
+                                             "events": n_events},
+            "cpu_baseline": {"value": val, "unit": "iters/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "%d full iteration(s) of the %s pair on the oracle restatement "
+                                       "(the reference rasterizer's native source is absent)" % (done, name)},
+            "e2e": {"value": val, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gsevt", choices=["gsevt", "reference"])
+    ap.add_argument("--workload", default="adjoint-500k-640x480", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    warmup = max(3, args.warmup)
+    prob = build_problem(args.workload, dev, seed_offset=rank)
+    bt = make_tracker(prob, dev)
+    hbm, peak_kind = measured_peaks()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # per-stage times and algorithmic bytes (one un-graphed iteration's stages)
+    stages = stage_times(bt)
+    algo = algorithmic_bytes(bt, prob)
+    top = max(stages, key=lambda k: stages[k])
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = time_batched(bt, args.steps, warmup, flush)
+    clk = clocks.stop()
+    ms = sum(times) / len(times)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    iters_per_s = 1000.0 / ms * bt.num
+    value = iters_per_s * world
+    e2e_ms, h2d, d2h = time_e2e(bt, prob, max(10, args.steps // 2), 3)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    plain_ms = None if args.no_plain else time_plain(prob, dev)
+    st, K = bt.check_status()
+
+    # CUDA-event timing of the dominant stage (its own launch stream), bytes / time
+    top_ms = stages[top]
+    achieved = algo[top] / (top_ms * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(args.workload, {}).get(top)
+        except Exception:
+            traffic = None
+    passes = (bt.frame.L.sort_bits + 7) // 8
+    launches_per_iter = 12 + passes
+    line = {
+        "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "gaussians": prob["n"], "width": prob["W"], "height": prob["H"],
+                   "events": WORKLOADS[args.workload][5], "hypotheses": bt.num, "views_per_launch": 2 * bt.num,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed (256 MB write) between timed iterations", "path": "batched adjoint, CUDA graph"},
+        "e2e": {"value": 1000.0 / e2e_ms * bt.num * world, "unit": "iters/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "plain": None if plain_ms is None else {"value": 1000.0 / plain_ms, "unit": "iters/s", "ms_per_step": plain_ms,
+                                                "batched_over_plain": (1000.0 / ms) / (1000.0 / plain_ms)},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": algo[top], "stage_ms": stages},
+        "counts": algo["counts"], "status": st,
+        "gpu_launches": launches_per_iter * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(prob)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

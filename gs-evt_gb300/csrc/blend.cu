@@ -1,0 +1,363 @@
+// Per-tile front-to-back alpha blending and its adjoint.
+//
+// One block of 256 threads per 16x16 tile (global tile ids cover every view of the
+// frame, so views of different sizes share the launch).  The tile's depth-sorted
+// Gaussians are staged through shared memory in batches of 256 records (32 bytes
+// each, or 48 with RGB); a batch is loaded with cp.async (16-byte global->shared copies
+// that bypass registers) while the block is still blending the previous one.  A pixel
+// stops when its transmittance would fall below 1e-4; the block stops when
+// __syncthreads_count says every pixel has stopped.
+//
+// Blending (the published 3DGS rule): alpha = min(0.99, o * exp(power)), skipped when
+// power > 0 or alpha < 1/255; C += c alpha T; T *= 1 - alpha.  exp is gs_expf, so the
+// per-pixel decisions and sums are bit-identical to the CPU oracle.
+//
+// Adjoint: the same front-to-back traversal with the same decisions (no per-pixel
+// contributor lists are stored); with P the running prefix of c alpha T and C the
+// stored pixel value,
+//   dC/dalpha_i = T_i c_i - (C - P_i + T_final bg) / (1 - alpha_i).
+// Per-Gaussian contributions are reduced across the warp in FP32 (shuffles), summed
+// per tile in shared memory and added to the global per-slot gradients once per tile.
+#include "common.cuh"
+
+namespace {
+
+struct BlendParams {
+    const gsevt_view *views;
+    int num_views;
+    const gsevt_pair *pairs;
+    Workspace ws;
+    const uint32_t *vals;  // sorted values (view, Gaussian) slots
+    int rgb;
+    int total_pixels;
+    float *image, *final_T, *depth, *alpha;
+    int32_t *n_contrib, *n_touched;
+    const float *dL_dimage, *dL_ddepth, *dL_dalpha;
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+struct Batch {
+    float4 A[GS_BLOCK];
+    float4 B[GS_BLOCK];
+    float4 C[GS_BLOCK];
+    uint32_t id[GS_BLOCK];
+};
+
+// Issue the copies of batch `r` of the tile range into buffer `buf`.
+__device__ __forceinline__ void load_batch(const BlendParams &p, Batch &buf, uint2 range, int r)
+{
+    uint32_t idx = range.x + (uint32_t)r * GS_BLOCK + threadIdx.x;
+    if (idx < range.y) {
+        uint32_t vg = __ldg(p.vals + idx);
+        buf.id[threadIdx.x] = vg;
+        cp_async16(&buf.A[threadIdx.x], p.ws.recA + vg);
+        cp_async16(&buf.B[threadIdx.x], p.ws.recB + vg);
+        if (p.rgb) cp_async16(&buf.C[threadIdx.x], p.ws.recC + vg);
+    }
+    cp_async_commit();
+}
+
+__global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
+{
+    __shared__ Batch sb[2];
+    __shared__ gsevt_view V;
+    const int tile = blockIdx.x;
+    if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
+    __syncthreads();
+    const int lt = tile - V.tile_offset;
+    const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
+    const int px = tx * GSEVT_TILE + (threadIdx.x & 15), py = ty * GSEVT_TILE + (threadIdx.x >> 4);
+    const bool inside = px < V.width && py < V.height;
+    const float pxf = (float)px, pyf = (float)py;
+    const uint2 range = p.ws.ranges[tile];
+    const int todo = (int)(range.y - range.x);
+    const int rounds = (todo + GS_BLOCK - 1) / GS_BLOCK;
+    float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f, Aacc = 0.0f;
+    int contributor = 0, last = 0;
+    bool done = !inside;
+    if (rounds > 0) load_batch(p, sb[0], range, 0);
+    for (int r = 0; r < rounds; ++r) {
+        Batch &cur = sb[r & 1];
+        if (r + 1 < rounds) {
+            load_batch(p, sb[(r + 1) & 1], range, r + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        if (__syncthreads_count(done) == GS_BLOCK) break;
+        const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
+        for (int j = 0; !done && j < n; ++j) {
+            ++contributor;
+            const float4 A = cur.A[j], B = cur.B[j];
+            const float dx = A.x - pxf, dy = A.y - pyf;
+            const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
+            if (power > 0.0f) continue;
+            // exp(-5.6) * 1 < 1/255: such Gaussians fail the alpha test anyway
+            if (power < -5.6f && B.w <= 1.0f) continue;
+            const float alpha = fminf(0.99f, B.w * gs_expf(power));
+            if (alpha < 1.0f / 255.0f) continue;
+            const float test_T = T * (1.0f - alpha);
+            if (test_T < 0.0001f) { done = true; break; }
+            if (p.rgb) {
+                const float4 Cc = cur.C[j];
+                C0 = C0 + (Cc.x * alpha) * T;
+                C1 = C1 + (Cc.y * alpha) * T;
+                C2 = C2 + (Cc.z * alpha) * T;
+            } else {
+                C0 = C0 + (A.w * alpha) * T;
+            }
+            D = D + (A.z * alpha) * T;
+            Aacc = Aacc + alpha * T;
+            if (p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
+            T = test_T;
+            last = contributor;
+        }
+        __syncthreads();  // the next iteration overwrites this buffer
+    }
+    cp_async_wait<0>();  // no copy may still target shared memory when the block exits
+    if (inside) {
+        const int pix = V.pix_offset + py * V.width + px;
+        const size_t P = (size_t)p.total_pixels;
+        if (p.rgb) {
+            p.image[pix] = C0 + T * V.bg[0];
+            p.image[P + pix] = C1 + T * V.bg[1];
+            p.image[2 * P + pix] = C2 + T * V.bg[2];
+        } else {
+            const float bgg = (0.2989f * V.bg[0] + 0.587f * V.bg[1]) + 0.114f * V.bg[2];
+            p.image[pix] = C0 + T * bgg;
+        }
+        p.final_T[pix] = T;
+        if (p.depth) p.depth[pix] = D;
+        if (p.alpha) p.alpha[pix] = Aacc;
+        if (p.n_contrib) p.n_contrib[pix] = last;
+    }
+}
+
+// number of per-Gaussian gradient components accumulated per tile
+#define NG_GREY 8
+#define NG_RGB 10
+
+template <bool RGB>
+__global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
+{
+    constexpr int NG = RGB ? NG_RGB : NG_GREY;
+    __shared__ Batch sb[2];
+    __shared__ float acc[GS_BLOCK][NG + 1];
+    __shared__ gsevt_view V;
+    const int tile = blockIdx.x;
+    if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
+    for (int i = threadIdx.x; i < GS_BLOCK * (NG + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int lt = tile - V.tile_offset;
+    const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
+    const int px = tx * GSEVT_TILE + (threadIdx.x & 15), py = ty * GSEVT_TILE + (threadIdx.x >> 4);
+    const bool inside = px < V.width && py < V.height;
+    const float pxf = (float)px, pyf = (float)py;
+    const uint2 range = p.ws.ranges[tile];
+    const int todo = (int)(range.y - range.x);
+    const int rounds = (todo + GS_BLOCK - 1) / GS_BLOCK;
+    const size_t P = (size_t)p.total_pixels;
+    const int pix = V.pix_offset + py * V.width + px;
+
+    // per-pixel inputs
+    float Tf = 1.0f, Cfg[3] = {0, 0, 0}, gC[3] = {0, 0, 0}, gD = 0.0f, gA = 0.0f, Dtot = 0.0f, Atot = 0.0f;
+    float bgc[3];
+    if (RGB) { bgc[0] = V.bg[0]; bgc[1] = V.bg[1]; bgc[2] = V.bg[2]; }
+    else { bgc[0] = (0.2989f * V.bg[0] + 0.587f * V.bg[1]) + 0.114f * V.bg[2]; bgc[1] = bgc[2] = 0.0f; }
+    if (inside) {
+        Tf = p.final_T[pix];
+#pragma unroll
+        for (int c = 0; c < (RGB ? 3 : 1); ++c) Cfg[c] = p.image[c * P + pix] - Tf * bgc[c];
+        if (p.dL_dimage) {
+#pragma unroll
+            for (int c = 0; c < (RGB ? 3 : 1); ++c) gC[c] = p.dL_dimage[c * P + pix];
+            if (p.dL_ddepth) { gD = p.dL_ddepth[pix]; Dtot = p.depth[pix]; }
+            if (p.dL_dalpha) { gA = p.dL_dalpha[pix]; Atot = p.alpha[pix]; }
+        } else if (V.pair >= 0) {
+            // gradient of the pair loss w.r.t. this view's grey image
+            const gsevt_pair &pr = p.pairs[V.pair];
+            const double *sc = p.ws.loss_scal + 4 * V.pair;
+            const double s = sc[0], cross = sc[1], L = sc[3];
+            const int lp = py * V.width + px;
+            const int other = V.pair_role == 0 ? pr.next_view : pr.last_view;
+            const float Io = p.image[p.views[other].pix_offset + lp];
+            const float Is = p.image[pix];
+            const float dI = V.pair_role == 0 ? (Io - Is) : (Is - Io);
+            const float e = pr.event[lp];
+            const float n = (float)((double)dI / s);
+            const float ng = (float)((1.0 - cross / s) / L);
+            float g;
+            if (pr.unsigned_mode) {
+                const float sg = (dI > 0.0f) ? 1.0f : (dI < 0.0f ? -1.0f : 0.0f);
+                g = sg * (fabsf(n) - fabsf(e)) / (float)L;
+            } else {
+                g = (n - e) / (float)L;
+            }
+            const float dd = (g - n * ng) / (float)s;
+            gC[0] = V.pair_role == 0 ? -dd : dd;
+        }
+    }
+
+    float T = 1.0f, Pc[3] = {0, 0, 0}, PD = 0.0f, PA = 0.0f;
+    bool done = !inside;
+    if (rounds > 0) load_batch(p, sb[0], range, 0);
+    for (int r = 0; r < rounds; ++r) {
+        Batch &cur = sb[r & 1];
+        if (r + 1 < rounds) {
+            load_batch(p, sb[(r + 1) & 1], range, r + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        if (__syncthreads_count(done) == GS_BLOCK) break;
+        const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
+        for (int j = 0; j < n; ++j) {
+            if (__all_sync(0xffffffffu, done)) break;
+            float gv[NG];
+#pragma unroll
+            for (int k = 0; k < NG; ++k) gv[k] = 0.0f;
+            bool contrib = false;
+            if (!done) {
+                const float4 A = cur.A[j], B = cur.B[j];
+                const float dx = A.x - pxf, dy = A.y - pyf;
+                const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
+                if (power <= 0.0f && !(power < -5.6f && B.w <= 1.0f)) {
+                    const float G = gs_expf(power);
+                    const float araw = B.w * G;
+                    const float alpha = fminf(0.99f, araw);
+                    if (alpha >= 1.0f / 255.0f) {
+                        const float test_T = T * (1.0f - alpha);
+                        if (test_T < 0.0001f) {
+                            done = true;
+                        } else {
+                            contrib = true;
+                            float col[3];
+                            if (RGB) { const float4 Cc = cur.C[j]; col[0] = Cc.x; col[1] = Cc.y; col[2] = Cc.z; }
+                            else { col[0] = A.w; col[1] = col[2] = 0.0f; }
+                            const float wgt = alpha * T;
+                            const float inv1m = 1.0f / (1.0f - alpha);
+                            float dal = 0.0f;
+#pragma unroll
+                            for (int c = 0; c < (RGB ? 3 : 1); ++c) {
+                                Pc[c] = Pc[c] + (col[c] * alpha) * T;
+                                const float suffix = (Cfg[c] - Pc[c]) + Tf * bgc[c];
+                                dal += gC[c] * (T * col[c] - suffix * inv1m);
+                            }
+                            PD = PD + (A.z * alpha) * T;
+                            PA = PA + alpha * T;
+                            dal += gD * (T * A.z - (Dtot - PD) * inv1m);
+                            dal += gA * (T - (Atot - PA) * inv1m);
+                            if (RGB) { gv[6] = gC[0] * wgt; gv[8] = gC[1] * wgt; gv[9] = gC[2] * wgt; }
+                            else gv[6] = gC[0] * wgt;
+                            gv[7] = gD * wgt;
+                            if (araw <= 0.99f) {
+                                gv[5] = dal * G;
+                                const float dpow = dal * araw;
+                                gv[2] = dpow * (-0.5f * dx * dx);
+                                gv[3] = dpow * (-dx * dy);
+                                gv[4] = dpow * (-0.5f * dy * dy);
+                                gv[0] = dpow * (-B.x * dx - B.y * dy);
+                                gv[1] = dpow * (-B.z * dy - B.y * dx);
+                            }
+                            T = test_T;
+                        }
+                    }
+                }
+            }
+            if (__any_sync(0xffffffffu, contrib)) {
+#pragma unroll
+                for (int k = 0; k < NG; ++k) {
+                    const float s = warp_sum(gv[k]);
+                    if (lane == 0 && s != 0.0f) atomicAdd(&acc[j][k], s);
+                }
+            }
+        }
+        __syncthreads();
+        // flush this batch's per-Gaussian sums to the global per-slot gradients
+        if (threadIdx.x < n) {
+            const uint32_t vg = cur.id[threadIdx.x];
+            float *gA4 = (float *)(p.ws.gradA + vg);
+            float *gB4 = (float *)(p.ws.gradB + vg);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float a = acc[threadIdx.x][k];
+                if (a != 0.0f) atomicAdd(gA4 + k, a);
+                acc[threadIdx.x][k] = 0.0f;
+            }
+            // gradB = {conic z, opacity, colour (grey or r), depth}
+            const int mapB[4] = {4, 5, 6, 7};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float a = acc[threadIdx.x][mapB[k]];
+                if (a != 0.0f) atomicAdd(gB4 + k, a);
+                acc[threadIdx.x][mapB[k]] = 0.0f;
+            }
+            if (RGB) {
+                float *gC4 = (float *)(p.ws.gradC + vg);
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    float a = acc[threadIdx.x][8 + k];
+                    if (a != 0.0f) atomicAdd(gC4 + k, a);
+                    acc[threadIdx.x][8 + k] = 0.0f;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    cp_async_wait<0>();
+}
+
+}  // namespace
+
+static BlendParams make_params(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals)
+{
+    BlendParams p;
+    p.views = f->views;
+    p.num_views = f->L.num_views;
+    p.pairs = f->pairs;
+    p.ws = ws;
+    p.vals = vals;
+    p.rgb = f->L.channels == 3;
+    p.total_pixels = f->L.total_pixels;
+    p.image = f->image;
+    p.final_T = f->final_T;
+    p.depth = f->depth;
+    p.alpha = f->alpha;
+    p.n_contrib = f->n_contrib;
+    p.n_touched = f->n_touched;
+    p.dL_dimage = p.dL_ddepth = p.dL_dalpha = nullptr;
+    return p;
+}
+
+int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s)
+{
+    if (f->L.total_tiles <= 0) return GSEVT_OK;
+    BlendParams p = make_params(f, ws, vals);
+    if (f->n_touched) cudaMemsetAsync(f->n_touched, 0, (size_t)f->L.num_vg * 4, s);
+    k_blend_fwd<<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    GS_CUDA_CHECK();
+    return GSEVT_OK;
+}
+
+int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, const float *dL_dimage,
+                        const float *dL_ddepth, const float *dL_dalpha, cudaStream_t s)
+{
+    if (f->L.total_tiles <= 0) return GSEVT_OK;
+    BlendParams p = make_params(f, ws, vals);
+    p.dL_dimage = dL_dimage;
+    p.dL_ddepth = dL_ddepth;
+    p.dL_dalpha = dL_dalpha;
+    if (p.rgb) k_blend_bwd<true><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    else k_blend_bwd<false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    GS_CUDA_CHECK();
+    return GSEVT_OK;
+}

@@ -1,0 +1,161 @@
+// Shared definitions of the gsevt CUDA library (sm_103a).
+//
+// Every translation unit is compiled with -fmad=false: a multiply followed by an add
+// is rounded twice unless an explicit fmaf() is written, so the forward arithmetic
+// reproduces the operation order of the CPU oracle bit for bit (keys, sort order,
+// tile ranges, radii and images compare exactly).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "gsevt.h"
+
+#define GS_BLOCK 256
+#define GS_SORT_KPT 12
+#define GS_SORT_TILE (GS_BLOCK * GS_SORT_KPT)
+#define GS_MAX_PASSES 8
+#define GS_SPIN_LIMIT (1u << 22)
+
+// ----------------------------------------------------------------- exp ----------
+// Deterministic exp for x <= 0: Cody & Waite (1980) reduction x = k ln2 + r with a
+// two-part ln2, degree-7 Taylor polynomial of e^r (Horner, fused multiply-adds) and an
+// exact power-of-two scale.  Bit-identical to or_expf in the CPU oracle.  Returns 0 for
+// x < -87 and for NaN.
+__host__ __device__ __forceinline__ float gs_expf(float x)
+{
+    if (!(x >= -87.0f)) return 0.0f;
+    float k = rintf(x * 0x1.715476p+0f);
+    float r = fmaf(k, -0x1.62e4p-1f, x);
+    r = fmaf(k, -0x1.7f7d1cp-20f, r);
+    float p = 0x1.a01a02p-13f;
+    p = fmaf(p, r, 0x1.6c16c2p-10f);
+    p = fmaf(p, r, 0x1.111112p-7f);
+    p = fmaf(p, r, 0x1.555556p-5f);
+    p = fmaf(p, r, 0x1.555556p-3f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    int ki = (int)k;
+#ifdef __CUDA_ARCH__
+    float sc = __int_as_float((ki + 127) << 23);
+#else
+    union { uint32_t u; float f; } cv;
+    cv.u = (uint32_t)(ki + 127) << 23;
+    float sc = cv.f;
+#endif
+    return p * sc;
+}
+
+// ------------------------------------------------------------ workspace ---------
+struct Workspace {
+    uint32_t *status;     // [0] status bits, [1] num keys, [2] sort epoch, [3] sorted buffer
+    int4 *bin;            // [num_vg] {touched, rect lo (x0 | y0<<16), rect hi, depth bits}
+    float4 *recA;         // [num_vg] {mean x, mean y, depth, grey}
+    float4 *recB;         // [num_vg] {conic x, y, z, opacity}
+    float4 *recC;         // [num_vg] {r, g, b, 0} (channels == 3)
+    float4 *gradA;        // [num_vg] dL/d{mean x, mean y, conic x, conic y}
+    float4 *gradB;        // [num_vg] dL/d{conic z, opacity, grey or r, depth}
+    float4 *gradC;        // [num_vg] dL/d{g, b, -, -} (channels == 3)
+    uint32_t *scan_sums;  // [num_scan_blocks]
+    uint32_t *scan_offs;  // [num_scan_blocks]
+    unsigned long long *keys[2];
+    uint32_t *vals[2];
+    uint32_t *sort_hist;      // [GS_MAX_PASSES][256]
+    uint32_t *sort_counter;   // [GS_MAX_PASSES]
+    unsigned long long *sort_lookback;  // [max sort tiles][256]  {epoch:32 | flag:2 | count:30}
+    uint2 *ranges;        // [total_tiles]
+    double *loss_part;    // [loss_blocks][4]
+    double *loss_scal;    // [num_pairs][4] {s, cross, e2, L}
+    uint32_t *loss_done;  // [num_pairs]
+    double *xi_part;      // [num_scan_blocks][6]
+    double *xi;           // [num_views][6]
+    size_t bytes;
+};
+
+__host__ __device__ inline size_t gs_align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+inline uint32_t gs_sort_tiles(uint32_t cap) { return (cap + GS_SORT_TILE - 1) / GS_SORT_TILE; }
+
+// Carves the workspace in a fixed order; with base == nullptr it only sizes it.
+inline Workspace gs_carve(const gsevt_layout &L, void *base)
+{
+    Workspace w;
+    char *p = (char *)base;
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> void * {
+        void *r = base ? (void *)(p + off) : nullptr;
+        off += gs_align(bytes > 0 ? bytes : 1);
+        return r;
+    };
+    size_t vg = (size_t)(L.num_vg > 0 ? L.num_vg : 1);
+    bool rgb = L.channels == 3;
+    w.status = (uint32_t *)take(64);
+    w.bin = (int4 *)take(vg * 16);
+    w.recA = (float4 *)take(vg * 16);
+    w.recB = (float4 *)take(vg * 16);
+    w.recC = rgb ? (float4 *)take(vg * 16) : nullptr;
+    w.gradA = (float4 *)take(vg * 16);
+    w.gradB = (float4 *)take(vg * 16);
+    w.gradC = rgb ? (float4 *)take(vg * 16) : nullptr;
+    w.scan_sums = (uint32_t *)take((size_t)L.num_scan_blocks * 4);
+    w.scan_offs = (uint32_t *)take((size_t)L.num_scan_blocks * 4);
+    size_t cap = (size_t)(L.key_capacity > 0 ? L.key_capacity : 1);
+    w.keys[0] = (unsigned long long *)take(cap * 8);
+    w.keys[1] = (unsigned long long *)take(cap * 8);
+    w.vals[0] = (uint32_t *)take(cap * 4);
+    w.vals[1] = (uint32_t *)take(cap * 4);
+    w.sort_hist = (uint32_t *)take(GS_MAX_PASSES * 256 * 4);
+    w.sort_counter = (uint32_t *)take(GS_MAX_PASSES * 4);
+    w.sort_lookback = (unsigned long long *)take((size_t)gs_sort_tiles((uint32_t)cap) * 256 * 8);
+    w.ranges = (uint2 *)take((size_t)L.total_tiles * 8);
+    w.loss_part = (double *)take((size_t)L.loss_blocks * 4 * 8);
+    w.loss_scal = (double *)take((size_t)L.num_pairs * 4 * 8);
+    w.loss_done = (uint32_t *)take((size_t)L.num_pairs * 4);
+    w.xi_part = (double *)take((size_t)L.num_scan_blocks * 6 * 8);
+    w.xi = (double *)take((size_t)L.num_views * 6 * 8);
+    w.bytes = off;
+    return w;
+}
+
+// ------------------------------------------------------------- helpers ----------
+__device__ __forceinline__ int gs_find_map(const gsevt_map *maps, int num_maps, int block)
+{
+    int m = 0;
+    for (int i = 1; i < num_maps; ++i)
+        if (maps[i].block_offset <= block) m = i;
+    return m;
+}
+
+// view containing global tile id `tile` (views ordered by tile_offset)
+__device__ __forceinline__ int gs_find_view_by_tile(const gsevt_view *views, int num_views, int tile)
+{
+    int lo = 0, hi = num_views - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (views[mid].tile_offset <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+#define GS_CUDA_CHECK()                                         \
+    do {                                                        \
+        cudaError_t _e = cudaGetLastError();                    \
+        if (_e != cudaSuccess) return GSEVT_ERR_CUDA;           \
+    } while (0)

@@ -1,0 +1,109 @@
+// Normalised intensity-change loss of every render pair, in one launch.
+//
+// Replaces utils/render_camera/frame.py:86-94 (dI = I_next - I_last, n = dI/||dI||,
+// |n|) and utils/tracker.py:93-103 (L = ||n - E|| or || |n| - |E| ||), which run as
+// ~8 forward and ~10 backward torch kernels per iteration.  With s = ||dI||,
+// c = sum(dI E) (signed) or sum(|dI| |E|) (unsigned) and e2 = sum(E^2),
+//   L^2 = 1 - 2 c / s + e2,
+// so one FP64 reduction pass gives L; the per-pixel gradient
+//   dL/dI_next = -dL/dI_last = (g - n (n.g)) / s,  n.g = (1 - c/s) / L,
+// is formed inside the blend adjoint from (s, c, L) without another pass.
+// Each block reduces a slice of one pair into FP64 partials; the last block of the
+// pair to finish (atomic ticket after a fence) adds the partials in a fixed order, so
+// the scalars do not depend on block scheduling.
+#include "common.cuh"
+
+namespace {
+
+#define LOSS_PIX_PER_THREAD 8
+
+__device__ __forceinline__ int find_pair(const gsevt_pair *pairs, int num_pairs, int block)
+{
+    int lo = 0, hi = num_pairs - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pairs[mid].block_offset <= block) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, const gsevt_pair *pairs, int num_pairs,
+                                                   const float *image, Workspace ws, double *loss_out)
+{
+    __shared__ double part[GS_BLOCK / 32][3];
+    __shared__ bool is_last;
+    const int b = blockIdx.x;
+    const int pi = find_pair(pairs, num_pairs, b);
+    const gsevt_pair pr = pairs[pi];
+    const gsevt_view &Vl = views[pr.last_view];
+    const gsevt_view &Vn = views[pr.next_view];
+    const int P = Vl.width * Vl.height;
+    const int lb = b - pr.block_offset;
+    double s2 = 0.0, cr = 0.0, e2 = 0.0;
+    const int base = lb * GS_BLOCK * LOSS_PIX_PER_THREAD;
+    for (int k = 0; k < LOSS_PIX_PER_THREAD; ++k) {
+        int i = base + k * GS_BLOCK + threadIdx.x;
+        if (i < P) {
+            float d = image[Vn.pix_offset + i] - image[Vl.pix_offset + i];
+            float e = pr.event[i];
+            s2 += (double)d * (double)d;
+            e2 += (double)e * (double)e;
+            cr += pr.unsigned_mode ? (double)fabsf(d) * (double)fabsf(e) : (double)d * (double)e;
+        }
+    }
+    s2 = warp_sum_d(s2);
+    cr = warp_sum_d(cr);
+    e2 = warp_sum_d(e2);
+    if ((threadIdx.x & 31) == 0) {
+        part[threadIdx.x >> 5][0] = s2;
+        part[threadIdx.x >> 5][1] = cr;
+        part[threadIdx.x >> 5][2] = e2;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) s += part[w][threadIdx.x];
+        ws.loss_part[(size_t)b * 4 + threadIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int t = atomicAdd(&ws.loss_done[pi], 1u);
+        is_last = (t == (unsigned)pr.num_blocks - 1u);
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        double S2 = 0, CR = 0, E2 = 0;
+        const volatile double *lp = ws.loss_part;
+        for (int i = 0; i < pr.num_blocks; ++i) {
+            size_t q = (size_t)(pr.block_offset + i) * 4;
+            S2 += lp[q];
+            CR += lp[q + 1];
+            E2 += lp[q + 2];
+        }
+        double s = sqrt(S2);
+        double L2 = 1.0 - 2.0 * CR / s + E2;
+        double L = sqrt(L2 > 0.0 ? L2 : 0.0);
+        ws.loss_scal[4 * pi + 0] = s;
+        ws.loss_scal[4 * pi + 1] = CR;
+        ws.loss_scal[4 * pi + 2] = E2;
+        ws.loss_scal[4 * pi + 3] = L;
+        if (loss_out) loss_out[pi] = L;
+        if (!(L == L) || !(s > 0.0)) atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
+        ws.loss_done[pi] = 0u;
+    }
+}
+
+}  // namespace
+
+int gs_loss_blocks_for(int pixels) { return (pixels + GS_BLOCK * LOSS_PIX_PER_THREAD - 1) / (GS_BLOCK * LOSS_PIX_PER_THREAD); }
+
+int gs_launch_loss(const gsevt_frame *f, const Workspace &ws, double *loss_out, cudaStream_t s)
+{
+    if (f->L.num_pairs <= 0 || f->L.loss_blocks <= 0 || !f->pairs) return GSEVT_ERR_ARG;
+    k_loss<<<f->L.loss_blocks, GS_BLOCK, 0, s>>>(f->views, f->pairs, f->L.num_pairs, f->image, ws, loss_out);
+    GS_CUDA_CHECK();
+    return GSEVT_OK;
+}

@@ -1,0 +1,225 @@
+// Onesweep LSD radix sort of (64-bit key, 32-bit value) pairs, 8-bit digits.
+//
+// Method: Adinets & Merrill, "Onesweep: A Faster Least Significant Digit Radix Sort
+// for GPUs" (2022).  One histogram kernel reads the keys once and counts the digits of
+// every pass; each pass is then a single kernel in which a block
+//   1. takes a tile ticket from an atomic counter (tickets are handed out in launch
+//      order, so every earlier tile belongs to a block that is already running),
+//   2. ranks its GS_SORT_TILE keys stably with warp-level match/ballot multisplit,
+//   3. publishes its per-digit counts to a look-back table and walks back over the
+//      earlier tiles (decoupled look-back) to get its exclusive per-digit prefix,
+//   4. scatters keys and values through shared memory to their global positions.
+// Look-back entries are single 64-bit words {epoch:32 | flag:2 | count:30}; the epoch
+// changes every pass, so the table never needs clearing between passes or sorts (it
+// must be zero-filled once, when the workspace is created).  Every wait on a
+// predecessor is bounded by GS_SPIN_LIMIT polls; on expiry the block records
+// GSEVT_STATUS_SORT_TIMEOUT and continues, so a fault can never hang the GPU.
+// Stability: ranks follow (warp, key slot, lane) order, which is the input order.
+#include "common.cuh"
+
+namespace {
+
+#define SORT_KPT GS_SORT_KPT
+#define SORT_TILE GS_SORT_TILE
+#define FLAG_AGG 1ull
+#define FLAG_PREFIX 2ull
+
+__global__ void k_sort_hist(const unsigned long long *keys, const uint32_t *status, uint32_t capacity,
+                            int passes, uint32_t *hist)
+{
+    __shared__ uint32_t sh[GS_MAX_PASSES][256];
+    for (int i = threadIdx.x; i < GS_MAX_PASSES * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    uint32_t K = min(status[1], capacity);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
+        unsigned long long k = keys[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8 * p)) & 255], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        uint32_t v = (&sh[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
+__global__ void k_sort_epoch(uint32_t *status, int passes)
+{
+    // status[2]: last epoch used; status[4]: first epoch of this sort
+    uint32_t e = status[2];
+    status[4] = e + 1;
+    status[2] = e + (uint32_t)passes;
+}
+
+struct PassParams {
+    const unsigned long long *kin;
+    const uint32_t *vin;
+    unsigned long long *kout;
+    uint32_t *vout;
+    const uint32_t *hist;       // this pass's 256 digit counts
+    uint32_t *counter;          // this pass's tile ticket counter
+    unsigned long long *lookback;
+    uint32_t *status;
+    uint32_t capacity;
+    int pass;
+};
+
+__global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams p)
+{
+    __shared__ unsigned long long skeys[SORT_TILE];
+    __shared__ uint32_t svals[SORT_TILE];
+    __shared__ uint32_t whist[GS_BLOCK / 32][256];
+    __shared__ uint32_t dstart[256];
+    __shared__ uint32_t gbase[256];
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t wscan[GS_BLOCK / 32];
+
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(p.counter, 1u);
+    for (int i = tid; i < (GS_BLOCK / 32) * 256; i += GS_BLOCK) (&whist[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t K = min(p.status[1], p.capacity);
+    const uint32_t tile = s_tile;
+    const uint32_t ntiles = (K + SORT_TILE - 1) / SORT_TILE;
+    if (tile >= ntiles) return;
+    const uint32_t base = tile * SORT_TILE;
+    const uint32_t count = min((uint32_t)SORT_TILE, K - base);
+    const int shift = 8 * p.pass;
+    const unsigned long long epoch = (unsigned long long)(p.status[4] + (uint32_t)p.pass);
+
+    unsigned long long key[SORT_KPT];
+    uint32_t val[SORT_KPT];
+    uint32_t rank[SORT_KPT];
+    int dig[SORT_KPT];
+#pragma unroll
+    for (int k = 0; k < SORT_KPT; ++k) {
+        uint32_t li = (uint32_t)(w * 32 * SORT_KPT + k * 32 + lane);
+        bool ok = li < count;
+        key[k] = ok ? p.kin[base + li] : 0ull;
+        val[k] = ok ? p.vin[base + li] : 0u;
+        dig[k] = ok ? (int)((key[k] >> shift) & 255) : 256;
+    }
+    const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < SORT_KPT; ++k) {
+        int d = dig[k];
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t before = 0;
+        int leader = __ffs(peers) - 1;
+        if (d < 256) before = whist[w][d];
+        __syncwarp();
+        if (d < 256 && lane == leader) whist[w][d] = before + __popc(peers);
+        __syncwarp();
+        rank[k] = before + __popc(peers & lt_mask);
+    }
+    __syncthreads();
+    // per digit: exclusive offsets across warps and the tile total
+    const int d = tid;  // GS_BLOCK == 256 digits
+    uint32_t total = 0;
+#pragma unroll
+    for (int i = 0; i < GS_BLOCK / 32; ++i) {
+        uint32_t t = whist[i][d];
+        whist[i][d] = total;
+        total += t;
+    }
+    // publish the tile aggregate (or the inclusive prefix for tile 0)
+    volatile unsigned long long *lb = (volatile unsigned long long *)p.lookback;
+    if (tile == 0) lb[d] = (epoch << 32) | (FLAG_PREFIX << 30) | total;
+    else lb[(size_t)tile * 256 + d] = (epoch << 32) | (FLAG_AGG << 30) | total;
+    // decoupled look-back
+    uint32_t excl = 0;
+    if (tile > 0) {
+        int t = (int)tile - 1;
+        uint32_t spins = 0;
+        while (t >= 0) {
+            unsigned long long e = lb[(size_t)t * 256 + d];
+            unsigned long long fl = (e >> 30) & 3ull;
+            if ((e >> 32) != epoch || fl == 0) {
+                if (++spins > GS_SPIN_LIMIT) {
+                    atomicOr(p.status, GSEVT_STATUS_SORT_TIMEOUT);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            excl += (uint32_t)(e & 0x3fffffffull);
+            if (fl == FLAG_PREFIX) break;
+            --t;
+        }
+        lb[(size_t)tile * 256 + d] = (epoch << 32) | (FLAG_PREFIX << 30) | (excl + total);
+    }
+    // global digit offset: exclusive scan of the pass histogram + tile prefix
+    uint32_t hcount = p.hist[d];
+    uint32_t inc = hcount, inc_t = total;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        uint32_t yt = __shfl_up_sync(0xffffffffu, inc_t, o);
+        if (lane >= o) { inc += y; inc_t += yt; }
+    }
+    __shared__ uint32_t wscan_t[GS_BLOCK / 32];
+    if (lane == 31) { wscan[w] = inc; wscan_t[w] = inc_t; }
+    __syncthreads();
+    uint32_t wb = 0, wbt = 0;
+    for (int i = 0; i < w; ++i) { wb += wscan[i]; wbt += wscan_t[i]; }
+    gbase[d] = (wb + inc - hcount) + excl;
+    dstart[d] = wbt + inc_t - total;
+    __syncthreads();
+    // scatter into shared memory in block-sorted order
+#pragma unroll
+    for (int k = 0; k < SORT_KPT; ++k) {
+        if (dig[k] < 256) {
+            uint32_t pos = dstart[dig[k]] + whist[w][dig[k]] + rank[k];
+            skeys[pos] = key[k];
+            svals[pos] = val[k];
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < count; i += GS_BLOCK) {
+        unsigned long long kk = skeys[i];
+        int dd = (int)((kk >> shift) & 255);
+        uint32_t pos = gbase[dd] + (i - dstart[dd]);
+        p.kout[pos] = kk;
+        p.vout[pos] = svals[i];
+    }
+}
+
+}  // namespace
+
+// Sorts ws.keys[0]/vals[0] (count in status[1]) on the low `bits` bits; the result is in
+// buffer index returned through *out_buf.  max_keys bounds the grid (host-known count, or
+// the capacity when the count is only known on the device).
+int gs_launch_sort(const gsevt_frame *f, const Workspace &ws, int bits, uint32_t max_keys, int *out_buf,
+                   cudaStream_t s)
+{
+    int passes = (bits + 7) / 8;
+    if (passes < 1) passes = 1;
+    if (passes > GS_MAX_PASSES) return GSEVT_ERR_ARG;
+    *out_buf = passes & 1;
+    if (max_keys > f->L.key_capacity) max_keys = f->L.key_capacity;
+    if (max_keys == 0) return GSEVT_OK;
+    cudaMemsetAsync(ws.sort_hist, 0, GS_MAX_PASSES * 256 * 4, s);
+    cudaMemsetAsync(ws.sort_counter, 0, GS_MAX_PASSES * 4, s);
+    GS_CUDA_CHECK();
+    int hblocks = (int)std::min<uint32_t>((max_keys + 1023) / 1024, 152u * 4u);
+    k_sort_hist<<<hblocks, 256, 0, s>>>(ws.keys[0], ws.status, f->L.key_capacity, passes, ws.sort_hist);
+    k_sort_epoch<<<1, 1, 0, s>>>(ws.status, passes);
+    GS_CUDA_CHECK();
+    uint32_t tiles = (max_keys + SORT_TILE - 1) / SORT_TILE;
+    for (int pass = 0; pass < passes; ++pass) {
+        PassParams p;
+        int src = pass & 1;
+        p.kin = ws.keys[src];
+        p.vin = ws.vals[src];
+        p.kout = ws.keys[src ^ 1];
+        p.vout = ws.vals[src ^ 1];
+        p.hist = ws.sort_hist + 256 * pass;
+        p.counter = ws.sort_counter + pass;
+        p.lookback = ws.sort_lookback;
+        p.status = ws.status;
+        p.capacity = f->L.key_capacity;
+        p.pass = pass;
+        k_sort_pass<<<tiles, GS_BLOCK, 0, s>>>(p);
+        GS_CUDA_CHECK();
+    }
+    return GSEVT_OK;
+}

@@ -1,0 +1,273 @@
+/*
+ * gsevt — C ABI of the GB300-native tracking hot path of GS-EVT (libgsevt.so).
+ *
+ * The reference binds its rasterizer as a Python extension of the absent submodule
+ * diff-gaussian-rasterization-vwRT (.gitmodules:1-3); its interface is known from the
+ * call sites gaussian_splatting/gaussian_renderer/__init__.py:313-383
+ * (GaussianRasterizationSettings fields :318-337, GaussianRasterizer forward
+ * arguments :362-375, 5-tuple return :362).  Each entry point below names the part of
+ * that interface, or of the tracker around it, that it replaces.
+ *
+ * Conventions
+ *   - All buffers are device memory owned by the caller, except the gsevt_frame /
+ *     gsevt_layout structs themselves, which are host memory read at call time.
+ *   - Work is enqueued on the stream passed in; calls return before the GPU finishes.
+ *   - Every call returns an int status (GSEVT_OK = 0 or a negative code).  Nothing
+ *     throws across the ABI.  Device-side failures (key-buffer overflow, a bounded
+ *     wait that ran out) are recorded in the frame's status words and read back with
+ *     gsevt_read_status.
+ *   - No entry point allocates device memory: scratch lives in the caller-provided
+ *     workspace sized by gsevt_workspace_bytes.
+ *   - Re-entrant per stream; no global mutable state.
+ */
+#ifndef GSEVT_H
+#define GSEVT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *gsevt_stream_t; /* = cudaStream_t */
+
+enum {
+    GSEVT_OK = 0,
+    GSEVT_ERR_ARG = -1,          /* bad shape, size or pointer */
+    GSEVT_ERR_KEY_OVERFLOW = -2, /* more (tile, Gaussian) pairs than the key capacity */
+    GSEVT_ERR_NONFINITE = -3,    /* non-finite loss or gradient */
+    GSEVT_ERR_TIMEOUT = -4,      /* a bounded device-side wait ran out */
+    GSEVT_ERR_CUDA = -5,         /* a CUDA launch or copy failed */
+    GSEVT_ERR_WORKSPACE = -6     /* workspace smaller than gsevt_workspace_bytes */
+};
+
+/* status word bits, in gsevt_read_status()[0] */
+#define GSEVT_STATUS_KEY_OVERFLOW 1u
+#define GSEVT_STATUS_SORT_TIMEOUT 2u
+#define GSEVT_STATUS_NONFINITE 4u
+
+#define GSEVT_TILE 16
+#define GSEVT_LOSS_PIXELS_PER_BLOCK 2048 /* pixels reduced by one loss block */
+#define GSEVT_MAP_PLANES 15 /* packed map: 15 float4 planes of n entries */
+
+/* One rendered view (device-resident table entry, 192 bytes).  Replaces the per-call
+ * GaussianRasterizationSettings record (gaussian_renderer/__init__.py:318-337):
+ * viewmatrix -> R, t; projmatrix_raw -> P; campos; tanfovx/y; bg; image size. */
+typedef struct gsevt_view {
+    float R[9];       /* world -> camera rotation, row-major */
+    float t[3];       /* world -> camera translation */
+    float P[16];      /* camera -> clip projection, row-major (projmatrix_raw^T) */
+    float campos[3];  /* camera centre in world coordinates */
+    float tanfovx, tanfovy;
+    float bg[3];      /* background colour (grey uses 0.2989/0.5870/0.1140 weights) */
+    int32_t width, height;
+    int32_t tiles_x, tiles_y;
+    int32_t tile_offset;  /* first global tile id of this view */
+    int32_t pix_offset;   /* first pixel of this view in per-pixel buffers */
+    int32_t map;          /* index into the map table */
+    int32_t vg_offset;    /* first (view, Gaussian) slot of this view */
+    int32_t sb_offset;    /* first scan block of this view */
+    int32_t pair;         /* render pair this view belongs to, or -1 */
+    int32_t pair_role;    /* 0: t (last), 1: t + dtau (next) */
+    int32_t pad;
+} gsevt_view;
+
+/* One Gaussian map (device-resident table entry).  Exactly one colour source
+ * (shs or colors) and one covariance source (scales+rotations or cov3d) or the packed
+ * planes, mirroring the rasterizer's "exactly one of" rules
+ * (gaussian_renderer/__init__.py:80-113). */
+typedef struct gsevt_map {
+    const float *xyz;        /* [n][3] means3D */
+    const float *opacity;    /* [n] activated opacity */
+    const float *scales;     /* [n][3] activated scales, or NULL */
+    const float *rotations;  /* [n][4] (w,x,y,z) normalised, or NULL */
+    const float *cov3d;      /* [n][6] cov3D_precomp, or NULL */
+    const float *shs;        /* [n][sh_coeffs][3], or NULL */
+    const float *colors;     /* [n][3] colors_precomp, or NULL */
+    const void *packed;      /* [15][n] float4 planes from gsevt_pack_map, or NULL */
+    int32_t n;
+    int32_t sh_degree;       /* active SH degree 0..3 */
+    int32_t sh_coeffs;       /* coefficients per channel in shs (>= (deg+1)^2) */
+    float scale_modifier;
+    int32_t first_view;      /* views of this map are contiguous in the view table */
+    int32_t num_views;
+    int32_t block_offset;    /* first preprocess block of this map */
+    int32_t pad;
+} gsevt_map;
+
+/* Per-map gradient outputs of gsevt_preprocess_bwd (all nullable; device pointers).
+ * Gradients are written (not accumulated) for every Gaussian of the map. */
+typedef struct gsevt_map_grads {
+    float *means3d;    /* [n][3] */
+    float *means2d;    /* [n][3] dL/d(NDC x, y), z = 0 (the means2D convention) */
+    float *opacity;    /* [n] */
+    float *scales;     /* [n][3] */
+    float *rotations;  /* [n][4] */
+    float *cov3d;      /* [n][6] */
+    float *shs;        /* [n][sh_coeffs][3] */
+    float *colors;     /* [n][3] */
+} gsevt_map_grads;
+
+/* A (t, t + dtau) render pair and its event frame (utils/render_camera/frame.py:86-94,
+ * utils/tracker.py:93-103). */
+typedef struct gsevt_pair {
+    int32_t last_view, next_view;
+    const float *event;      /* [H][W] event frame: signed, or |E| when unsigned_mode */
+    int32_t unsigned_mode;   /* 0: L = ||n - E||, 1: L = || |n| - |E| || */
+    int32_t pose;            /* pose state this pair belongs to (batched tracker) */
+    int32_t block_offset;    /* first loss-reduction block of this pair */
+    int32_t num_blocks;
+} gsevt_pair;
+
+/* Sizes of one rendering frame (host struct). */
+typedef struct gsevt_layout {
+    int32_t num_views, num_maps, num_pairs;
+    int32_t num_vg;             /* sum over views of the view's map size */
+    int32_t num_scan_blocks;    /* sum over views of ceil(n / 256) */
+    int32_t preprocess_blocks;  /* sum over maps of ceil(n / 256) */
+    int32_t total_tiles, total_pixels;
+    int32_t channels;           /* 3 = RGB (drop-in), 1 = grey (tracker) */
+    int32_t sort_bits;          /* 32 + bits of (total_tiles - 1) */
+    uint32_t key_capacity;      /* max (tile, Gaussian) pairs */
+    int32_t loss_blocks;        /* sum over pairs of loss-reduction blocks */
+} gsevt_layout;
+
+/* One rendering frame: layout, device tables, workspace and caller-owned outputs. */
+typedef struct gsevt_frame {
+    gsevt_layout L;
+    const gsevt_view *views;   /* device [num_views] */
+    const gsevt_map *maps;     /* device [num_maps] */
+    const gsevt_pair *pairs;   /* device [num_pairs] or NULL */
+    void *workspace;           /* device, gsevt_workspace_bytes(&L) */
+    size_t workspace_bytes;
+    float *image;              /* [channels][total_pixels] */
+    float *final_T;            /* [total_pixels] */
+    float *depth;              /* [total_pixels] or NULL */
+    float *alpha;              /* [total_pixels] or NULL */
+    int32_t *n_contrib;        /* [total_pixels] or NULL */
+    int32_t *radii;            /* [num_vg] or NULL */
+    int32_t *n_touched;        /* [num_vg] or NULL */
+} gsevt_frame;
+
+/* ---- sizing ---- */
+size_t gsevt_workspace_bytes(const gsevt_layout *L);
+/* Zero the parts of a fresh workspace that must start at zero (status words, sort
+ * look-back table, loss tickets).  Call once after allocating it. */
+int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream);
+/* sizeof of the ABI structs, for binding checks: view, map, map_grads, pair, layout,
+ * frame, pose_state (7 entries).  Touches no GPU state. */
+void gsevt_abi_sizes(int32_t *out7);
+/* Byte offsets of the workspace regions for a layout (introspection for tests and
+ * tools), in this order: status, bin, recA, recB, recC, gradA, gradB, gradC,
+ * scan_sums, scan_offs, keys0, keys1, vals0, vals1, sort_hist, sort_counter,
+ * sort_lookback, ranges, loss_part, loss_scal, loss_done, xi_part, xi (23 entries;
+ * absent regions are reported as UINT64_MAX).  Touches no GPU state. */
+void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out23);
+
+/* ---- map packing ----
+ * Replaces the per-call activation + torch.cat of get_features
+ * (gaussian_renderer/__init__.py:277-297, gaussian_model.py:75-95): packs a map once
+ * into 15 float4 planes {x,y,z,opacity}, {cov xx,xy,xz,yy}, {yz,zz,0,0}, 12 x SH. */
+int gsevt_pack_map(int32_t n, const float *xyz, const float *opacity, const float *scales,
+                   const float *rotations, const float *cov3d, const float *shs,
+                   int32_t sh_coeffs, float scale_modifier, void *packed, gsevt_stream_t stream);
+
+/* ---- forward stages (GaussianRasterizer.forward, gaussian_renderer/__init__.py:362-375) ----
+ * preprocess: per (view, Gaussian) projection, EWA conic, radius, tile rect, SH colour.
+ * Also writes radii (the forward's 2nd return value) when frame->radii is set. */
+int gsevt_preprocess_fwd(const gsevt_frame *f, gsevt_stream_t stream);
+/* key duplication, onesweep radix sort of (view|tile|depth) keys, tile ranges.
+ * max_keys bounds the sort grid: the host-known key count (after gsevt_read_status),
+ * or 0 to size it from the key capacity (no host sync; CUDA-graph friendly). */
+int gsevt_bin_and_sort(const gsevt_frame *f, uint32_t max_keys, gsevt_stream_t stream);
+/* per-tile front-to-back blend: image, final T, depth, opacity, n_touched */
+int gsevt_blend_fwd(const gsevt_frame *f, gsevt_stream_t stream);
+
+/* ---- loss (utils/render_camera/frame.py:86-94 + utils/tracker.py:93-103) ----
+ * Per pair reductions in FP64; loss_out[p] = L of pair p (device doubles). */
+int gsevt_loss_fwd(const gsevt_frame *f, double *loss_out, gsevt_stream_t stream);
+
+/* ---- backward (GaussianRasterizer backward, implicit in loss.backward(),
+ *      utils/tracker.py:212) ----
+ * blend adjoint: per-Gaussian 2D gradients.  dL_dimage ([channels][total_pixels]) etc.
+ * come from the caller (drop-in); when dL_dimage is NULL the per-pixel gradient is
+ * formed from the pair losses computed by gsevt_loss_fwd (tracker). */
+int gsevt_blend_bwd(const gsevt_frame *f, const float *dL_dimage, const float *dL_ddepth,
+                    const float *dL_dalpha, gsevt_stream_t stream);
+/* preprocess adjoint: per-view left-twist gradient xi_out[v][6] = dL/d(rho, theta) of
+ * view v (FP32 per Gaussian, warp-reduced, FP64 across blocks), plus map gradients
+ * for map m into grads[m] (host array of num_maps structs, nullable). */
+int gsevt_preprocess_bwd(const gsevt_frame *f, double *xi_out, const gsevt_map_grads *grads,
+                         gsevt_stream_t stream);
+
+/* Chain one view's twist gradient to the 12 optimised deltas of the drop-in call
+ * (theta, rho, w, v: gaussian_renderer/__init__.py:301-304) using the settings'
+ * vel_transofrm (4x4, transposed as passed, :266-269), delta_time (:270-271) and the
+ * current velocities (:331-332).  Exact SE(3) adjoint and left Jacobian, FP64.
+ * out12 = [theta(3), rho(3), w(3), v(3)] as float, written (not accumulated). */
+int gsevt_chain_view_grad(const double *xi, const float *vel_transform_t, float delta_time,
+                          const float *linear_vel, const float *angular_vel, float *out12,
+                          gsevt_stream_t stream);
+
+/* Build a view entry on the device from the drop-in settings tensors without a host
+ * sync: viewmatrix (4x4, transposed world_view_transform), projmatrix_raw (4x4,
+ * transposed), campos[3], bg[3]. */
+int gsevt_view_from_settings(const float *viewmatrix_t, const float *projmatrix_raw_t,
+                             const float *campos, const float *bg, float tanfovx, float tanfovy,
+                             int32_t width, int32_t height, int32_t tile_offset,
+                             int32_t pix_offset, int32_t map, int32_t vg_offset,
+                             int32_t sb_offset, gsevt_view *view_out, gsevt_stream_t stream);
+
+/* Copy the frame's status words to host (synchronises the stream):
+ * out[0] = status bits, out[1] = number of keys (tile, Gaussian pairs). */
+int gsevt_read_status(const gsevt_frame *f, uint32_t *out2, gsevt_stream_t stream);
+/* Clear the status words (enqueued on the stream). */
+int gsevt_clear_status(const gsevt_frame *f, gsevt_stream_t stream);
+
+/* ---- event frame (utils/event_camera/event.py:116-128, tracker.py:78-91) ----
+ * count += +1/-1 per event (int32 atomics), separable ksize Gaussian blur
+ * (sigma = 0.3((ksize-1)/2 - 1) + 0.8, replicate border), L2 normalisation,
+ * |E|, and nearest-neighbour pyramid levels.  out_signed / out_unsigned hold the
+ * levels back to back: level l is int(W*0.5^l) x int(H*0.5^l).  scratch must hold
+ * gsevt_event_scratch_bytes(W, H). */
+size_t gsevt_event_scratch_bytes(int32_t width, int32_t height);
+int gsevt_events_accumulate(int64_t n, const uint16_t *x, const uint16_t *y,
+                            const uint8_t *polarity, int32_t width, int32_t height,
+                            int32_t ksize, int32_t levels, void *scratch, float *out_signed,
+                            float *out_unsigned, gsevt_stream_t stream);
+
+/* ---- batched tracker iteration (utils/tracker.py:176-240) ----
+ * Per pose state (one tracking hypothesis / sequence): FP64 pose, velocity, Adam
+ * moments.  One call = render all pairs, loss, adjoint, exact chain to
+ * (theta, rho, w, v), Adam step with the reference's four parameter groups, pose and
+ * velocity update, and rewrite of the pose's two view-table entries. */
+typedef struct gsevt_pose_state {
+    double R[9], t[3];           /* current world -> camera pose */
+    double lin_vel[3], ang_vel[3];
+    double delta_tau;
+    double m[12], v[12];         /* Adam moments: theta, rho, w, v */
+    double lr[4];                /* base learning rates theta, rho, w, v */
+    double lr_scale[4];          /* current multipliers (velocity ramp) */
+    int32_t step[4];             /* Adam step per group */
+    int32_t opt_vel;             /* 0: coarse stage (theta, rho), 1: fine stage (all 12) */
+    int32_t last_view, next_view;
+    int32_t iter;
+    int32_t pad;
+    float fx, fy;                /* focal lengths of the rendered views */
+    double loss;                 /* last loss */
+    double grad[12];             /* last gradient (theta, rho, w, v) */
+} gsevt_pose_state;
+
+/* poses: device array.  Pair p's loss goes to loss_out[p] (device, nullable). */
+int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *poses, int32_t num_poses,
+                             double *loss_out, gsevt_stream_t stream);
+/* Write the two view entries (pose R, t, campos) of every pose from its state; the
+ * other view fields (size, projection, offsets, pair) are set by the caller. */
+int gsevt_track_init_views(gsevt_view *views, const gsevt_pose_state *poses, int32_t num_poses,
+                           gsevt_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GSEVT_H */

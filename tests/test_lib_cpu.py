@@ -1,0 +1,61 @@
+"""CPU checks of the C-ABI library: it loads, exports every entry point declared in
+include/gsevt.h, its struct sizes match the Python binding, and argument validation
+answers without touching a GPU."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from gsevt import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "gsevt.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gsevt_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    names = _declared()
+    assert len(names) >= 19
+    for n in names:
+        assert hasattr(L, n), n
+    assert sorted(_lib.EXPORTED) == names
+
+
+def test_abi_struct_sizes_match():
+    sizes = _lib.check_abi()
+    assert sizes[0] == 192  # gsevt_view
+
+
+def test_workspace_sizing_and_offsets():
+    L = _lib.Layout()
+    L.num_views, L.num_maps, L.num_pairs = 2, 1, 1
+    L.num_vg, L.num_scan_blocks, L.preprocess_blocks = 1000, 8, 4
+    L.total_tiles, L.total_pixels, L.channels, L.sort_bits = 24, 6144, 1, 37
+    L.key_capacity, L.loss_blocks = 100000, 3
+    small = _lib.lib().gsevt_workspace_bytes(C.byref(L))
+    L.key_capacity = 200000
+    big = _lib.lib().gsevt_workspace_bytes(C.byref(L))
+    assert big > small + 100000 * 24
+    off = _lib.workspace_offsets(L)
+    assert off["status"] == 0 and off["recC"] is None and off["gradC"] is None
+    seen = [v for v in off.values() if v is not None]
+    assert seen == sorted(seen) and all(v % 256 == 0 for v in seen)
+
+
+def test_argument_validation_without_gpu():
+    L = _lib.lib()
+    assert L.gsevt_preprocess_fwd(None, None) == -1
+    f = _lib.Frame()
+    f.L.num_views = 0
+    assert L.gsevt_bin_and_sort(C.byref(f), 0, None) == -1
+    assert L.gsevt_events_accumulate(10, None, None, None, 64, 48, 9, 3, None, None, None, None) == -1
+    assert L.gsevt_events_accumulate(0, None, None, None, 64, 48, 8, 1, C.c_void_p(16), C.c_void_p(16), None,
+                                     None) == -1  # even kernel size
+    assert L.gsevt_pack_map(10, None, None, None, None, None, None, 16, 1.0, None, None) == -1
+    assert L.gsevt_chain_view_grad(None, None, 0.0, None, None, None, None) == -1
