@@ -375,6 +375,21 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_profile(args):
+    import torch
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    prob = build_problem(args.workload, dev)
+    bt = make_tracker(prob, dev)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup + args.steps):
+        bt.step()
+    torch.cuda.synchronize()
+    st, k = bt.check_status()
+    print(json.dumps({"mode": "profile", "workload": args.workload, "iterations": args.warmup + args.steps,
+                      "keys": k, "status": st}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -384,9 +399,14 @@ def main():
     ap.add_argument("--workload", default="adjoint-500k-640x480", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
+                    help="profile: build the workload, then run warmup + steps un-graphed iterations "
+                         "(for ncu launch lists; prints no timings)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "profile":
+        return run_profile(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

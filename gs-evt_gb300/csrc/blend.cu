@@ -18,6 +18,11 @@
 //   dC/dalpha_i = T_i c_i - (C - P_i + T_final bg) / (1 - alpha_i).
 // Per-Gaussian contributions are reduced across the warp in FP32 (shuffles), summed
 // per tile in shared memory and added to the global per-slot gradients once per tile.
+//
+// Warp-level culling (both directions): each batch Gaussian gets a conservative pixel
+// box of its alpha support (gauss_box); a warp ballots which of them overlap its 16x2
+// pixel strip and walks only those, in depth order.  Gaussians outside the box cannot
+// pass the per-pixel alpha test, so the decisions and results are unchanged.
 #include "common.cuh"
 
 namespace {
@@ -48,8 +53,32 @@ struct Batch {
     float4 A[GS_BLOCK];
     float4 B[GS_BLOCK];
     float4 C[GS_BLOCK];
+    float4 box[GS_BLOCK];  // {xmin, xmax, ymin, ymax}: outside it the Gaussian fails the alpha test
     uint32_t id[GS_BLOCK];
 };
+
+// Conservative pixel box of a Gaussian's alpha support.  A pixel blends the Gaussian
+// only if alpha = min(0.99, o exp(power)) >= 1/255, i.e. -power <= tau = ln(255 o).  With
+// M the conic, -power = d^T M d / 2 in exact arithmetic; the FP32 evaluation of the six
+// products and sums deviates by less than 1e-6 tr(M) |d|^2, so every pixel that can pass
+// satisfies d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the slack also covers gs_expf's
+// 2 ulp and logf).  The box of that ellipse, widened by 0.1 % + 0.5 px, therefore never
+// excludes a pixel whose per-pixel test would pass, so culling against it leaves every
+// blending decision - and the result bits - unchanged.
+__device__ __forceinline__ float4 gauss_box(float4 A, float4 B)
+{
+    const float o = B.w;
+    if (!(o >= (1.0f / 255.0f) * 0.999f)) return make_float4(1e30f, -1e30f, 1e30f, -1e30f);
+    const float tau = logf(255.0f * o) * 1.0001f + 1e-3f;
+    const float g = 1e-6f * (fabsf(B.x) + fabsf(B.z));
+    const float a = 0.5f * B.x - g, b = 0.5f * B.y, c = 0.5f * B.z - g;
+    const float det = a * c - b * b;
+    if (!(a > 0.0f && c > 0.0f && det > 0.0f && tau > -1e29f && tau < 1e29f))
+        return make_float4(-1e30f, 1e30f, -1e30f, 1e30f);  // no culling
+    const float hx = sqrtf(fmaxf(tau, 0.0f) * c / det) * 1.001f + 0.5f;
+    const float hy = sqrtf(fmaxf(tau, 0.0f) * a / det) * 1.001f + 0.5f;
+    return make_float4(A.x - hx, A.x + hx, A.y - hy, A.y + hy);
+}
 
 // Issue the copies of batch `r` of the tile range into buffer `buf`.
 __device__ __forceinline__ void load_batch(const BlendParams &p, Batch &buf, uint2 range, int r)
@@ -81,8 +110,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
     const int todo = (int)(range.y - range.x);
     const int rounds = (todo + GS_BLOCK - 1) / GS_BLOCK;
     float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f, Aacc = 0.0f;
-    int contributor = 0, last = 0;
+    int last = 0;
     bool done = !inside;
+    // this warp's pixel strip: full tile width, rows 2w and 2w + 1
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const float sx0 = (float)(tx * GSEVT_TILE), sx1 = sx0 + (float)(GSEVT_TILE - 1);
+    const float sy0 = (float)(ty * GSEVT_TILE + 2 * w), sy1 = sy0 + 1.0f;
     if (rounds > 0) load_batch(p, sb[0], range, 0);
     for (int r = 0; r < rounds; ++r) {
         Batch &cur = sb[r & 1];
@@ -94,31 +127,45 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
         }
         if (__syncthreads_count(done) == GS_BLOCK) break;
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
-        for (int j = 0; !done && j < n; ++j) {
-            ++contributor;
-            const float4 A = cur.A[j], B = cur.B[j];
-            const float dx = A.x - pxf, dy = A.y - pyf;
-            const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
-            if (power > 0.0f) continue;
-            // exp(-5.6) * 1 < 1/255: such Gaussians fail the alpha test anyway
-            if (power < -5.6f && B.w <= 1.0f) continue;
-            const float alpha = fminf(0.99f, B.w * gs_expf(power));
-            if (alpha < 1.0f / 255.0f) continue;
-            const float test_T = T * (1.0f - alpha);
-            if (test_T < 0.0001f) { done = true; break; }
-            if (p.rgb) {
-                const float4 Cc = cur.C[j];
-                C0 = C0 + (Cc.x * alpha) * T;
-                C1 = C1 + (Cc.y * alpha) * T;
-                C2 = C2 + (Cc.z * alpha) * T;
-            } else {
-                C0 = C0 + (A.w * alpha) * T;
+        if ((int)threadIdx.x < n) cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x]);
+        __syncthreads();
+        bool warp_done = false;
+        for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
+            // candidates of this warp among the next 32 Gaussians, in depth order
+            bool hit = false;
+            if (c0 + lane < n) {
+                const float4 bx = cur.box[c0 + lane];
+                hit = bx.y >= sx0 && bx.x <= sx1 && bx.w >= sy0 && bx.z <= sy1;
             }
-            D = D + (A.z * alpha) * T;
-            Aacc = Aacc + alpha * T;
-            if (p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
-            T = test_T;
-            last = contributor;
+            unsigned mask = __ballot_sync(0xffffffffu, hit);
+            while (mask) {
+                if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
+                const int j = c0 + __ffs(mask) - 1;
+                mask &= mask - 1;
+                if (done) continue;
+                const float4 A = cur.A[j], B = cur.B[j];
+                const float dx = A.x - pxf, dy = A.y - pyf;
+                const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
+                // power > 0, or exp(-5.6) * 1 < 1/255 (fails the alpha test anyway): skip
+                if (power > 0.0f || (power < -5.6f && B.w <= 1.0f)) continue;
+                const float alpha = fminf(0.99f, B.w * gs_expf(power));
+                if (alpha < 1.0f / 255.0f) continue;
+                const float test_T = T * (1.0f - alpha);
+                if (test_T < 0.0001f) { done = true; continue; }
+                if (p.rgb) {
+                    const float4 Cc = cur.C[j];
+                    C0 = C0 + (Cc.x * alpha) * T;
+                    C1 = C1 + (Cc.y * alpha) * T;
+                    C2 = C2 + (Cc.z * alpha) * T;
+                } else {
+                    C0 = C0 + (A.w * alpha) * T;
+                }
+                D = D + (A.z * alpha) * T;
+                Aacc = Aacc + alpha * T;
+                if (p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
+                T = test_T;
+                last = r * GS_BLOCK + j + 1;
+            }
         }
         __syncthreads();  // the next iteration overwrites this buffer
     }
@@ -141,27 +188,34 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
     }
 }
 
-// number of per-Gaussian gradient components accumulated per tile
-#define NG_GREY 8
-#define NG_RGB 10
+// Per-Gaussian gradient components accumulated per tile:
+//   0,1 mean x,y (pixels)  2,3,4 conic x,y,z  5 opacity  6 colour (grey or r)  7 depth
+//   8,9 colour g,b (RGB only).
+// Modes: 0 tracker (grey, pose only: 0-4 and 6), 1 grey drop-in (0-7), 2 RGB drop-in (0-9).
+template <int MODE> struct Comps { static constexpr int n = MODE == 0 ? 6 : (MODE == 1 ? 8 : 10); };
+template <int MODE>
+__device__ __forceinline__ constexpr int comp_idx(int q) { return (MODE == 0 && q >= 5) ? 6 : q; }
 
-template <bool RGB>
+template <int MODE>
 __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
 {
-    constexpr int NG = RGB ? NG_RGB : NG_GREY;
+    constexpr bool RGB = MODE == 2;
+    constexpr int NC = Comps<MODE>::n;
     __shared__ Batch sb[2];
-    __shared__ float acc[GS_BLOCK][NG + 1];
+    __shared__ float acc[GS_BLOCK][NC + 1];
     __shared__ gsevt_view V;
     const int tile = blockIdx.x;
     if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
-    for (int i = threadIdx.x; i < GS_BLOCK * (NG + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
+    for (int i = threadIdx.x; i < GS_BLOCK * (NC + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
     __syncthreads();
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int lt = tile - V.tile_offset;
     const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
     const int px = tx * GSEVT_TILE + (threadIdx.x & 15), py = ty * GSEVT_TILE + (threadIdx.x >> 4);
     const bool inside = px < V.width && py < V.height;
     const float pxf = (float)px, pyf = (float)py;
+    const float sx0 = (float)(tx * GSEVT_TILE), sx1 = sx0 + (float)(GSEVT_TILE - 1);
+    const float sy0 = (float)(ty * GSEVT_TILE + 2 * w), sy1 = sy0 + 1.0f;
     const uint2 range = p.ws.ranges[tile];
     const int todo = (int)(range.y - range.x);
     const int rounds = (todo + GS_BLOCK - 1) / GS_BLOCK;
@@ -177,7 +231,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         Tf = p.final_T[pix];
 #pragma unroll
         for (int c = 0; c < (RGB ? 3 : 1); ++c) Cfg[c] = p.image[c * P + pix] - Tf * bgc[c];
-        if (p.dL_dimage) {
+        if (MODE != 0) {
 #pragma unroll
             for (int c = 0; c < (RGB ? 3 : 1); ++c) gC[c] = p.dL_dimage[c * P + pix];
             if (p.dL_ddepth) { gD = p.dL_ddepth[pix]; Dtot = p.depth[pix]; }
@@ -220,95 +274,95 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         }
         if (__syncthreads_count(done) == GS_BLOCK) break;
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
-        for (int j = 0; j < n; ++j) {
-            if (__all_sync(0xffffffffu, done)) break;
-            float gv[NG];
+        if ((int)threadIdx.x < n) cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x]);
+        __syncthreads();
+        bool warp_done = false;
+        for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
+            bool hit = false;
+            if (c0 + lane < n) {
+                const float4 bx = cur.box[c0 + lane];
+                hit = bx.y >= sx0 && bx.x <= sx1 && bx.w >= sy0 && bx.z <= sy1;
+            }
+            unsigned mask = __ballot_sync(0xffffffffu, hit);
+            while (mask) {
+                if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
+                const int j = c0 + __ffs(mask) - 1;
+                mask &= mask - 1;
+                float gv[10];
 #pragma unroll
-            for (int k = 0; k < NG; ++k) gv[k] = 0.0f;
-            bool contrib = false;
-            if (!done) {
-                const float4 A = cur.A[j], B = cur.B[j];
-                const float dx = A.x - pxf, dy = A.y - pyf;
-                const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
-                if (power <= 0.0f && !(power < -5.6f && B.w <= 1.0f)) {
-                    const float G = gs_expf(power);
-                    const float araw = B.w * G;
-                    const float alpha = fminf(0.99f, araw);
-                    if (alpha >= 1.0f / 255.0f) {
-                        const float test_T = T * (1.0f - alpha);
-                        if (test_T < 0.0001f) {
-                            done = true;
-                        } else {
-                            contrib = true;
-                            float col[3];
-                            if (RGB) { const float4 Cc = cur.C[j]; col[0] = Cc.x; col[1] = Cc.y; col[2] = Cc.z; }
-                            else { col[0] = A.w; col[1] = col[2] = 0.0f; }
-                            const float wgt = alpha * T;
-                            const float inv1m = 1.0f / (1.0f - alpha);
-                            float dal = 0.0f;
+                for (int k = 0; k < 10; ++k) gv[k] = 0.0f;
+                bool contrib = false;
+                if (!done) {
+                    const float4 A = cur.A[j], B = cur.B[j];
+                    const float dx = A.x - pxf, dy = A.y - pyf;
+                    const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
+                    if (power <= 0.0f && !(power < -5.6f && B.w <= 1.0f)) {
+                        const float G = gs_expf(power);
+                        const float araw = B.w * G;
+                        const float alpha = fminf(0.99f, araw);
+                        if (alpha >= 1.0f / 255.0f) {
+                            const float test_T = T * (1.0f - alpha);
+                            if (test_T < 0.0001f) {
+                                done = true;
+                            } else {
+                                contrib = true;
+                                float col[3];
+                                if (RGB) { const float4 Cc = cur.C[j]; col[0] = Cc.x; col[1] = Cc.y; col[2] = Cc.z; }
+                                else { col[0] = A.w; col[1] = col[2] = 0.0f; }
+                                const float wgt = alpha * T;
+                                const float inv1m = 1.0f / (1.0f - alpha);
+                                float dal = 0.0f;
 #pragma unroll
-                            for (int c = 0; c < (RGB ? 3 : 1); ++c) {
-                                Pc[c] = Pc[c] + (col[c] * alpha) * T;
-                                const float suffix = (Cfg[c] - Pc[c]) + Tf * bgc[c];
-                                dal += gC[c] * (T * col[c] - suffix * inv1m);
+                                for (int c = 0; c < (RGB ? 3 : 1); ++c) {
+                                    Pc[c] = Pc[c] + (col[c] * alpha) * T;
+                                    const float suffix = (Cfg[c] - Pc[c]) + Tf * bgc[c];
+                                    dal += gC[c] * (T * col[c] - suffix * inv1m);
+                                }
+                                if (MODE != 0) {
+                                    PD = PD + (A.z * alpha) * T;
+                                    PA = PA + alpha * T;
+                                    dal += gD * (T * A.z - (Dtot - PD) * inv1m);
+                                    dal += gA * (T - (Atot - PA) * inv1m);
+                                    gv[7] = gD * wgt;
+                                }
+                                gv[6] = gC[0] * wgt;
+                                if (RGB) { gv[8] = gC[1] * wgt; gv[9] = gC[2] * wgt; }
+                                if (araw <= 0.99f) {
+                                    gv[5] = dal * G;
+                                    const float dpow = dal * araw;
+                                    gv[2] = dpow * (-0.5f * dx * dx);
+                                    gv[3] = dpow * (-dx * dy);
+                                    gv[4] = dpow * (-0.5f * dy * dy);
+                                    gv[0] = dpow * (-B.x * dx - B.y * dy);
+                                    gv[1] = dpow * (-B.z * dy - B.y * dx);
+                                }
+                                T = test_T;
                             }
-                            PD = PD + (A.z * alpha) * T;
-                            PA = PA + alpha * T;
-                            dal += gD * (T * A.z - (Dtot - PD) * inv1m);
-                            dal += gA * (T - (Atot - PA) * inv1m);
-                            if (RGB) { gv[6] = gC[0] * wgt; gv[8] = gC[1] * wgt; gv[9] = gC[2] * wgt; }
-                            else gv[6] = gC[0] * wgt;
-                            gv[7] = gD * wgt;
-                            if (araw <= 0.99f) {
-                                gv[5] = dal * G;
-                                const float dpow = dal * araw;
-                                gv[2] = dpow * (-0.5f * dx * dx);
-                                gv[3] = dpow * (-dx * dy);
-                                gv[4] = dpow * (-0.5f * dy * dy);
-                                gv[0] = dpow * (-B.x * dx - B.y * dy);
-                                gv[1] = dpow * (-B.z * dy - B.y * dx);
-                            }
-                            T = test_T;
                         }
                     }
                 }
-            }
-            if (__any_sync(0xffffffffu, contrib)) {
+                if (__any_sync(0xffffffffu, contrib)) {
 #pragma unroll
-                for (int k = 0; k < NG; ++k) {
-                    const float s = warp_sum(gv[k]);
-                    if (lane == 0 && s != 0.0f) atomicAdd(&acc[j][k], s);
+                    for (int q = 0; q < NC; ++q) {
+                        const float s = warp_sum(gv[comp_idx<MODE>(q)]);
+                        if (lane == 0 && s != 0.0f) atomicAdd(&acc[j][q], s);
+                    }
                 }
             }
         }
         __syncthreads();
         // flush this batch's per-Gaussian sums to the global per-slot gradients
-        if (threadIdx.x < n) {
+        if ((int)threadIdx.x < n) {
             const uint32_t vg = cur.id[threadIdx.x];
-            float *gA4 = (float *)(p.ws.gradA + vg);
-            float *gB4 = (float *)(p.ws.gradB + vg);
+            float *dst[10] = {(float *)(p.ws.gradA + vg), (float *)(p.ws.gradA + vg) + 1, (float *)(p.ws.gradA + vg) + 2,
+                              (float *)(p.ws.gradA + vg) + 3, (float *)(p.ws.gradB + vg), (float *)(p.ws.gradB + vg) + 1,
+                              (float *)(p.ws.gradB + vg) + 2, (float *)(p.ws.gradB + vg) + 3,
+                              RGB ? (float *)(p.ws.gradC + vg) : nullptr, RGB ? (float *)(p.ws.gradC + vg) + 1 : nullptr};
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                float a = acc[threadIdx.x][k];
-                if (a != 0.0f) atomicAdd(gA4 + k, a);
-                acc[threadIdx.x][k] = 0.0f;
-            }
-            // gradB = {conic z, opacity, colour (grey or r), depth}
-            const int mapB[4] = {4, 5, 6, 7};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                float a = acc[threadIdx.x][mapB[k]];
-                if (a != 0.0f) atomicAdd(gB4 + k, a);
-                acc[threadIdx.x][mapB[k]] = 0.0f;
-            }
-            if (RGB) {
-                float *gC4 = (float *)(p.ws.gradC + vg);
-#pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    float a = acc[threadIdx.x][8 + k];
-                    if (a != 0.0f) atomicAdd(gC4 + k, a);
-                    acc[threadIdx.x][8 + k] = 0.0f;
-                }
+            for (int q = 0; q < NC; ++q) {
+                const float a = acc[threadIdx.x][q];
+                if (a != 0.0f) atomicAdd(dst[comp_idx<MODE>(q)], a);
+                acc[threadIdx.x][q] = 0.0f;
             }
         }
         __syncthreads();
@@ -356,8 +410,9 @@ int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     p.dL_dimage = dL_dimage;
     p.dL_ddepth = dL_ddepth;
     p.dL_dalpha = dL_dalpha;
-    if (p.rgb) k_blend_bwd<true><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
-    else k_blend_bwd<false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    if (p.rgb) k_blend_bwd<2><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    else if (dL_dimage) k_blend_bwd<1><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    else k_blend_bwd<0><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

@@ -1,7 +1,9 @@
-// FP64 pose algebra on the device: the exact chain from per-view twist gradients to the
+// Pose algebra on the device: the exact chain from per-view twist gradients to the
 // reference's 12 optimised deltas, the Adam step and the pose / velocity update of the
 // batched tracker, and the drop-in helpers (view entry from settings tensors, chain of
-// one view's gradient).
+// one view's gradient).  The per-view gradient sums arrive in FP64 (the one FP64
+// reduction of the path); the chain, Adam and exponential maps run in FP32, as the
+// reference's own pose parameters do, and the pose itself is stored and composed in FP64.
 //
 // Pose conventions follow the reference:
 //   SE3_exp([rho, theta]) with the SO(3) left Jacobian V (utils/pose.py:26-91);
@@ -19,20 +21,24 @@
 
 namespace {
 
-struct M3 { double a[9]; };
+// 3x3 matrices in FP32: transcendental and divide-heavy math stays off the (slow) FP64
+// units; the per-view gradient sums arrive in FP64 and the pose is stored in FP64.
+struct M3 { float a[9]; };
 
-__device__ inline M3 m3_eye() { M3 r; for (int i = 0; i < 9; ++i) r.a[i] = (i % 4 == 0) ? 1.0 : 0.0; return r; }
+__device__ inline M3 m3_eye() { M3 r; for (int i = 0; i < 9; ++i) r.a[i] = (i % 4 == 0) ? 1.0f : 0.0f; return r; }
 __device__ inline M3 m3_mul(const M3 &x, const M3 &y)
 {
     M3 r;
+#pragma unroll
     for (int i = 0; i < 3; ++i)
+#pragma unroll
         for (int j = 0; j < 3; ++j)
             r.a[3 * i + j] = x.a[3 * i] * y.a[j] + x.a[3 * i + 1] * y.a[3 + j] + x.a[3 * i + 2] * y.a[6 + j];
     return r;
 }
-__device__ inline M3 m3_add(const M3 &x, const M3 &y, double sy) { M3 r; for (int i = 0; i < 9; ++i) r.a[i] = x.a[i] + sy * y.a[i]; return r; }
-__device__ inline M3 m3_scale(const M3 &x, double s) { M3 r; for (int i = 0; i < 9; ++i) r.a[i] = s * x.a[i]; return r; }
-__device__ inline M3 skew(const double *v)
+__device__ inline M3 m3_add(const M3 &x, const M3 &y, float sy) { M3 r; for (int i = 0; i < 9; ++i) r.a[i] = x.a[i] + sy * y.a[i]; return r; }
+__device__ inline M3 m3_scale(const M3 &x, float s) { M3 r; for (int i = 0; i < 9; ++i) r.a[i] = s * x.a[i]; return r; }
+__device__ inline M3 skew(const float *v)
 {
     M3 r;
     r.a[0] = 0; r.a[1] = -v[2]; r.a[2] = v[1];
@@ -40,35 +46,51 @@ __device__ inline M3 skew(const double *v)
     r.a[6] = -v[1]; r.a[7] = v[0]; r.a[8] = 0;
     return r;
 }
-__device__ inline void m3_vec(const M3 &m, const double *v, double *o)
+__device__ inline void m3_vec(const M3 &m, const float *v, float *o)
 {
     for (int i = 0; i < 3; ++i) o[i] = m.a[3 * i] * v[0] + m.a[3 * i + 1] * v[1] + m.a[3 * i + 2] * v[2];
 }
-__device__ inline void m3t_vec(const M3 &m, const double *v, double *o)
+__device__ inline void m3t_vec(const M3 &m, const float *v, float *o)
 {
     for (int i = 0; i < 3; ++i) o[i] = m.a[i] * v[0] + m.a[3 + i] * v[1] + m.a[6 + i] * v[2];
 }
 
-// SO3_exp with the reference's small-angle branch (utils/pose.py:26-41)
-__device__ inline M3 so3_exp(const double *th)
+// SO(3) coefficients sin(a)/a, (1-cos a)/a^2, (a - sin a)/a^3 with Taylor series below
+// 0.1 rad, where the closed forms lose accuracy in FP32 through cancellation.
+__device__ inline void so3_coeffs(float a, float &A, float &B, float &Cc)
 {
-    M3 W = skew(th), W2 = m3_mul(W, W);
-    double a = sqrt(th[0] * th[0] + th[1] * th[1] + th[2] * th[2]);
-    if (a < 1e-5) return m3_add(m3_add(m3_eye(), W, 1.0), W2, 0.5);
-    return m3_add(m3_add(m3_eye(), W, sin(a) / a), W2, (1.0 - cos(a)) / (a * a));
+    float a2 = a * a;
+    if (a < 0.1f) {
+        A = 1.0f - a2 * (1.0f / 6.0f) + a2 * a2 * (1.0f / 120.0f);
+        B = 0.5f - a2 * (1.0f / 24.0f) + a2 * a2 * (1.0f / 720.0f);
+        Cc = (1.0f / 6.0f) - a2 * (1.0f / 120.0f) + a2 * a2 * (1.0f / 5040.0f);
+    } else {
+        float s = sinf(a), c = cosf(a);
+        A = s / a;
+        B = (1.0f - c) / a2;
+        Cc = (a - s) / (a2 * a);
+    }
 }
 
-// V(theta) (utils/pose.py:61-76)
-__device__ inline M3 so3_jl(const double *th)
+__device__ inline M3 so3_exp(const float *th)
 {
     M3 W = skew(th), W2 = m3_mul(W, W);
-    double a = sqrt(th[0] * th[0] + th[1] * th[1] + th[2] * th[2]);
-    if (a < 1e-5) return m3_add(m3_add(m3_eye(), W, 0.5), W2, 1.0 / 6.0);
-    return m3_add(m3_add(m3_eye(), W, (1.0 - cos(a)) / (a * a)), W2, (a - sin(a)) / (a * a * a));
+    float A, B, Cc;
+    so3_coeffs(sqrtf(th[0] * th[0] + th[1] * th[1] + th[2] * th[2]), A, B, Cc);
+    return m3_add(m3_add(m3_eye(), W, A), W2, B);
+}
+
+// SO(3) left Jacobian V(theta) (utils/pose.py:61-76)
+__device__ inline M3 so3_jl(const float *th)
+{
+    M3 W = skew(th), W2 = m3_mul(W, W);
+    float A, B, Cc;
+    so3_coeffs(sqrtf(th[0] * th[0] + th[1] * th[1] + th[2] * th[2]), A, B, Cc);
+    return m3_add(m3_add(m3_eye(), W, B), W2, Cc);
 }
 
 // SE3_exp(xi = [rho, theta]) -> R, t
-__device__ inline void se3_exp(const double *xi, M3 &R, double *t)
+__device__ inline void se3_exp(const float *xi, M3 &R, float *t)
 {
     R = so3_exp(xi + 3);
     M3 V = so3_jl(xi + 3);
@@ -76,27 +98,30 @@ __device__ inline void se3_exp(const double *xi, M3 &R, double *t)
 }
 
 // Q block of the SE(3) left Jacobian
-__device__ inline M3 se3_q(const double *xi)
+__device__ inline M3 se3_q(const float *xi)
 {
-    const double *rho = xi, *phi = xi + 3;
+    const float *rho = xi, *phi = xi + 3;
     M3 P = skew(phi), Rh = skew(rho);
     M3 PR = m3_mul(P, Rh), RP = m3_mul(Rh, P), PRP = m3_mul(PR, P);
     M3 PPR = m3_mul(P, PR), RPP = m3_mul(RP, P);
     M3 PRPP = m3_mul(PRP, P), PPRP = m3_mul(P, PRP);
-    double a = sqrt(phi[0] * phi[0] + phi[1] * phi[1] + phi[2] * phi[2]);
-    double c1, c2, c3;
-    if (a < 1e-4) {
-        c1 = 1.0 / 6.0; c2 = 1.0 / 24.0; c3 = 1.0 / 120.0;
+    float a = sqrtf(phi[0] * phi[0] + phi[1] * phi[1] + phi[2] * phi[2]);
+    float a2 = a * a;
+    float c1, c2, c3;
+    if (a < 0.1f) {
+        c1 = (1.0f / 6.0f) - a2 * (1.0f / 120.0f) + a2 * a2 * (1.0f / 5040.0f);
+        c2 = (1.0f / 24.0f) - a2 * (1.0f / 720.0f) + a2 * a2 * (1.0f / 40320.0f);
+        c3 = (1.0f / 120.0f) - a2 * (1.0f / 2520.0f) + a2 * a2 * (1.0f / 120960.0f);
     } else {
-        double a2 = a * a, a3 = a2 * a, a4 = a3 * a, a5 = a4 * a;
-        c1 = (a - sin(a)) / a3;
-        c2 = (a2 + 2.0 * cos(a) - 2.0) / (2.0 * a4);
-        c3 = (2.0 * a - 3.0 * sin(a) + a * cos(a)) / (2.0 * a5);
+        float s = sinf(a), c = cosf(a), a3 = a2 * a, a4 = a3 * a, a5 = a4 * a;
+        c1 = (a - s) / a3;
+        c2 = (a2 + 2.0f * c - 2.0f) / (2.0f * a4);
+        c3 = (2.0f * a - 3.0f * s + a * c) / (2.0f * a5);
     }
-    M3 A = m3_add(m3_add(PR, RP, 1.0), PRP, 1.0);
-    M3 B = m3_add(m3_add(PPR, RPP, 1.0), PRP, -3.0);
-    M3 C = m3_add(PRPP, PPRP, 1.0);
-    M3 Q = m3_scale(Rh, 0.5);
+    M3 A = m3_add(m3_add(PR, RP, 1.0f), PRP, 1.0f);
+    M3 B = m3_add(m3_add(PPR, RPP, 1.0f), PRP, -3.0f);
+    M3 C = m3_add(PRPP, PPRP, 1.0f);
+    M3 Q = m3_scale(Rh, 0.5f);
     Q = m3_add(Q, A, c1);
     Q = m3_add(Q, B, c2);
     Q = m3_add(Q, C, c3);
@@ -104,50 +129,50 @@ __device__ inline M3 se3_q(const double *xi)
 }
 
 // out6 += Ad(E)^T g  with E = (R, t): Ad = [[R, [t]x R], [0, R]]  (twists [rho, theta])
-__device__ inline void adjoint_t_acc(const M3 &R, const double *t, const double *g, double *out6)
+__device__ inline void adjoint_t_acc(const M3 &R, const float *t, const float *g, float *out6)
 {
-    double a[3], b[3], c[3];
-    m3t_vec(R, g, a);                 // R^T g_rho
-    M3 tx = skew(t);
-    M3 txR = m3_mul(tx, R);
-    m3t_vec(txR, g, b);               // ([t]x R)^T g_rho
-    m3t_vec(R, g + 3, c);             // R^T g_theta
+    float a[3], b[3], c[3];
+    m3t_vec(R, g, a);
+    M3 txR = m3_mul(skew(t), R);
+    m3t_vec(txR, g, b);
+    m3t_vec(R, g + 3, c);
     for (int i = 0; i < 3; ++i) { out6[i] += a[i]; out6[3 + i] += b[i] + c[i]; }
 }
 
 // out6 += sc * J_l(xi)^T g,  J_l = [[J, Q], [0, J]]
-__device__ inline void jl_t_acc(const double *xi, const double *g, double sc, double *out6)
+__device__ inline void jl_t_acc(const float *xi, const float *g, float sc, float *out6)
 {
     M3 J = so3_jl(xi + 3), Q = se3_q(xi);
-    double a[3], b[3], c[3];
+    float a[3], b[3], c[3];
     m3t_vec(J, g, a);
     m3t_vec(Q, g, b);
     m3t_vec(J, g + 3, c);
     for (int i = 0; i < 3; ++i) { out6[i] += sc * a[i]; out6[3 + i] += sc * (b[i] + c[i]); }
 }
 
-__device__ inline void write_view_pose(gsevt_view *V, const M3 &R, const double *t)
+// rendered pose of role s (-1 last, +1 next): E_s T, with E_s = SE3_exp(s h [v, w]);
+// the product with the stored FP64 pose is formed in FP64.
+__device__ inline void pair_pose(const gsevt_pose_state &S, float sgn, double *Rs, double *ts, M3 &RE, float *tE)
 {
-    for (int i = 0; i < 9; ++i) V->R[i] = (float)R.a[i];
-    for (int i = 0; i < 3; ++i) V->t[i] = (float)t[i];
-    double c[3];
-    m3t_vec(R, t, c);
-    for (int i = 0; i < 3; ++i) V->campos[i] = (float)(-c[i]);
+    float h = (float)(S.delta_tau * 0.5);
+    float u[6] = {sgn * h * (float)S.lin_vel[0], sgn * h * (float)S.lin_vel[1], sgn * h * (float)S.lin_vel[2],
+                  sgn * h * (float)S.ang_vel[0], sgn * h * (float)S.ang_vel[1], sgn * h * (float)S.ang_vel[2]};
+    se3_exp(u, RE, tE);
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            Rs[3 * i + j] = (double)RE.a[3 * i] * S.R[j] + (double)RE.a[3 * i + 1] * S.R[3 + j] +
+                            (double)RE.a[3 * i + 2] * S.R[6 + j];
+        ts[i] = (double)RE.a[3 * i] * S.t[0] + (double)RE.a[3 * i + 1] * S.t[1] + (double)RE.a[3 * i + 2] * S.t[2] +
+                (double)tE[i];
+    }
 }
 
-// rendered pose of role s (-1 last, +1 next): E_s T
-__device__ inline void pair_pose(const gsevt_pose_state &S, double sgn, M3 &Rs, double *ts, M3 &RE, double *tE)
+__device__ inline void write_view_pose(gsevt_view *V, const double *R, const double *t)
 {
-    double h = S.delta_tau * 0.5;
-    double u[6] = {sgn * h * S.lin_vel[0], sgn * h * S.lin_vel[1], sgn * h * S.lin_vel[2],
-                   sgn * h * S.ang_vel[0], sgn * h * S.ang_vel[1], sgn * h * S.ang_vel[2]};
-    se3_exp(u, RE, tE);
-    M3 R;
-    for (int i = 0; i < 9; ++i) R.a[i] = S.R[i];
-    Rs = m3_mul(RE, R);
-    double Et[3];
-    m3_vec(RE, S.t, Et);
-    for (int i = 0; i < 3; ++i) ts[i] = Et[i] + tE[i];
+    for (int i = 0; i < 9; ++i) V->R[i] = (float)R[i];
+    for (int i = 0; i < 3; ++i) V->t[i] = (float)t[i];
+    for (int i = 0; i < 3; ++i)
+        V->campos[i] = (float)(-(R[i] * t[0] + R[3 + i] * t[1] + R[6 + i] * t[2]));
 }
 
 __global__ void k_track_finalize(gsevt_view *views, gsevt_pose_state *poses, int num_poses, Workspace ws,
@@ -155,82 +180,87 @@ __global__ void k_track_finalize(gsevt_view *views, gsevt_pose_state *poses, int
 {
     int pi = blockIdx.x * blockDim.x + threadIdx.x;
     if (pi >= num_poses) return;
-    gsevt_pose_state S = poses[pi];
-    double h = S.delta_tau * 0.5;
-    double gpose[6] = {0, 0, 0, 0, 0, 0}, gvel[6] = {0, 0, 0, 0, 0, 0};
+    gsevt_pose_state &S = poses[pi];
+    const float h = (float)(S.delta_tau * 0.5);
+    float gpose[6] = {0, 0, 0, 0, 0, 0}, gvel[6] = {0, 0, 0, 0, 0, 0};
     const int vids[2] = {S.last_view, S.next_view};
-    const double sg[2] = {-1.0, 1.0};
+    const float sg[2] = {-1.0f, 1.0f};
     for (int k = 0; k < 2; ++k) {
-        const double *g = ws.xi + 6 * vids[k];
-        M3 Rs, RE;
-        double ts[3], tE[3];
-        pair_pose(S, sg[k], Rs, ts, RE, tE);
+        float g[6];
+        for (int i = 0; i < 6; ++i) g[i] = (float)ws.xi[6 * vids[k] + i];
+        float u[6] = {sg[k] * h * (float)S.lin_vel[0], sg[k] * h * (float)S.lin_vel[1], sg[k] * h * (float)S.lin_vel[2],
+                      sg[k] * h * (float)S.ang_vel[0], sg[k] * h * (float)S.ang_vel[1], sg[k] * h * (float)S.ang_vel[2]};
+        M3 RE;
+        float tE[3];
+        se3_exp(u, RE, tE);
         adjoint_t_acc(RE, tE, g, gpose);
-        double u[6] = {sg[k] * h * S.lin_vel[0], sg[k] * h * S.lin_vel[1], sg[k] * h * S.lin_vel[2],
-                       sg[k] * h * S.ang_vel[0], sg[k] * h * S.ang_vel[1], sg[k] * h * S.ang_vel[2]};
         jl_t_acc(u, g, sg[k] * h, gvel);
     }
     // 12-vector in the reference's group order: theta, rho, w, v
-    double grad[12];
+    float grad[12];
     for (int i = 0; i < 3; ++i) {
         grad[i] = gpose[3 + i];
         grad[3 + i] = gpose[i];
         grad[6 + i] = gvel[3 + i];
         grad[9 + i] = gvel[i];
     }
-    for (int i = 0; i < 12; ++i) S.grad[i] = grad[i];
+    for (int i = 0; i < 12; ++i) S.grad[i] = (double)grad[i];
     for (int p = 0; p < num_pairs; ++p)
         if (pairs[p].pose == pi) S.loss = loss ? loss[p] : ws.loss_scal[4 * p + 3];
     bool finite = true;
     for (int i = 0; i < 12; ++i) finite &= isfinite(grad[i]);
     if (!finite) {
         atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
-        poses[pi] = S;
         return;
     }
-    // Adam (torch semantics): param starts at 0 every step (deltas are reset after the update)
-    double delta[12];
-    const double b1 = 0.9, b2 = 0.999, eps = 1e-8;
+    // Adam with torch's update rule; the parameter is 0 before every step (the deltas are
+    // reset after each update), so the new delta is the step itself
+    float delta[12];
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     for (int gi = 0; gi < 4; ++gi) {
         bool active = gi < 2 || S.opt_vel;
-        for (int k = 0; k < 3; ++k) delta[3 * gi + k] = 0.0;
+        for (int k = 0; k < 3; ++k) delta[3 * gi + k] = 0.0f;
         if (!active) continue;
         S.step[gi] += 1;
-        double bc1 = 1.0 - pow(b1, (double)S.step[gi]);
-        double bc2 = 1.0 - pow(b2, (double)S.step[gi]);
-        double lr = S.lr[gi] * S.lr_scale[gi];
+        float bc1 = 1.0f - powf(b1, (float)S.step[gi]);
+        float bc2 = 1.0f - powf(b2, (float)S.step[gi]);
+        float lr = (float)(S.lr[gi] * S.lr_scale[gi]);
         for (int k = 0; k < 3; ++k) {
             int i = 3 * gi + k;
-            S.m[i] = b1 * S.m[i] + (1.0 - b1) * grad[i];
-            S.v[i] = b2 * S.v[i] + (1.0 - b2) * grad[i] * grad[i];
-            double denom = sqrt(S.v[i]) / sqrt(bc2) + eps;
-            delta[i] = -(lr / bc1) * S.m[i] / denom;
+            float m = b1 * (float)S.m[i] + (1.0f - b1) * grad[i];
+            float v = b2 * (float)S.v[i] + (1.0f - b2) * grad[i] * grad[i];
+            S.m[i] = m;
+            S.v[i] = v;
+            float denom = sqrtf(v) / sqrtf(bc2) + eps;
+            delta[i] = -(lr / bc1) * m / denom;
         }
     }
     // update_vwRT: velocity first, then the pose
     if (S.opt_vel)
         for (int k = 0; k < 3; ++k) { S.ang_vel[k] += delta[6 + k]; S.lin_vel[k] += delta[9 + k]; }
-    double xi[6] = {delta[3], delta[4], delta[5], delta[0], delta[1], delta[2]};
+    float xi[6] = {delta[3], delta[4], delta[5], delta[0], delta[1], delta[2]};
     M3 Rd;
-    double td[3];
+    float td[3];
     se3_exp(xi, Rd, td);
-    M3 R;
-    for (int i = 0; i < 9; ++i) R.a[i] = S.R[i];
-    M3 Rn = m3_mul(Rd, R);
-    double tn[3];
-    m3_vec(Rd, S.t, tn);
-    for (int i = 0; i < 3; ++i) tn[i] += td[i];
-    for (int i = 0; i < 9; ++i) S.R[i] = Rn.a[i];
+    double Rn[9], tn[3];
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j)
+            Rn[3 * i + j] = (double)Rd.a[3 * i] * S.R[j] + (double)Rd.a[3 * i + 1] * S.R[3 + j] +
+                            (double)Rd.a[3 * i + 2] * S.R[6 + j];
+        tn[i] = (double)Rd.a[3 * i] * S.t[0] + (double)Rd.a[3 * i + 1] * S.t[1] + (double)Rd.a[3 * i + 2] * S.t[2] +
+                (double)td[i];
+    }
+    for (int i = 0; i < 9; ++i) S.R[i] = Rn[i];
     for (int i = 0; i < 3; ++i) S.t[i] = tn[i];
     S.iter += 1;
     // rewrite the pair's view entries for the next iteration
     for (int k = 0; k < 2; ++k) {
-        M3 Rs, RE;
-        double ts[3], tE[3];
+        double Rs[9], ts[3];
+        M3 RE;
+        float tE[3];
         pair_pose(S, sg[k], Rs, ts, RE, tE);
         write_view_pose(views + vids[k], Rs, ts);
     }
-    poses[pi] = S;
 }
 
 // Initialise the two view entries of every pose from its current state.
@@ -238,12 +268,13 @@ __global__ void k_track_views(gsevt_view *views, const gsevt_pose_state *poses, 
 {
     int pi = blockIdx.x * blockDim.x + threadIdx.x;
     if (pi >= num_poses) return;
-    gsevt_pose_state S = poses[pi];
+    const gsevt_pose_state &S = poses[pi];
     const int vids[2] = {S.last_view, S.next_view};
-    const double sg[2] = {-1.0, 1.0};
+    const float sg[2] = {-1.0f, 1.0f};
     for (int k = 0; k < 2; ++k) {
-        M3 Rs, RE;
-        double ts[3], tE[3];
+        double Rs[9], ts[3];
+        M3 RE;
+        float tE[3];
         pair_pose(S, sg[k], Rs, ts, RE, tE);
         write_view_pose(views + vids[k], Rs, ts);
     }
@@ -253,21 +284,21 @@ __global__ void k_chain_view(const double *xi, const float *E_t, float dt, const
                              float *out12)
 {
     M3 R;
-    double t[3];
+    float t[3], g[6];
     // E_t is the transposed 4x4 (row-major storage of E^T): E[i][j] = E_t[4 j + i]
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) R.a[3 * i + j] = (double)E_t[4 * j + i];
-    for (int i = 0; i < 3; ++i) t[i] = (double)E_t[12 + i];
-    double gpose[6] = {0, 0, 0, 0, 0, 0}, gvel[6] = {0, 0, 0, 0, 0, 0};
-    adjoint_t_acc(R, t, xi, gpose);
-    double d = (double)dt;
-    double u[6] = {d * lin[0], d * lin[1], d * lin[2], d * ang[0], d * ang[1], d * ang[2]};
-    if (d != 0.0) jl_t_acc(u, xi, d, gvel);
+        for (int j = 0; j < 3; ++j) R.a[3 * i + j] = E_t[4 * j + i];
+    for (int i = 0; i < 3; ++i) t[i] = E_t[12 + i];
+    for (int i = 0; i < 6; ++i) g[i] = (float)xi[i];
+    float gpose[6] = {0, 0, 0, 0, 0, 0}, gvel[6] = {0, 0, 0, 0, 0, 0};
+    adjoint_t_acc(R, t, g, gpose);
+    float u[6] = {dt * lin[0], dt * lin[1], dt * lin[2], dt * ang[0], dt * ang[1], dt * ang[2]};
+    if (dt != 0.0f) jl_t_acc(u, g, dt, gvel);
     for (int i = 0; i < 3; ++i) {
-        out12[i] = (float)gpose[3 + i];
-        out12[3 + i] = (float)gpose[i];
-        out12[6 + i] = (float)gvel[3 + i];
-        out12[9 + i] = (float)gvel[i];
+        out12[i] = gpose[3 + i];
+        out12[3 + i] = gpose[i];
+        out12[6 + i] = gvel[3 + i];
+        out12[9 + i] = gvel[i];
     }
 }
 

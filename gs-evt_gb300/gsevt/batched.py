@@ -57,9 +57,10 @@ class BatchedTracker:
                 t = lambda a: torch.as_tensor(np.asarray(a) if not torch.is_tensor(a) else a,
                                               dtype=torch.float32).to(self.device).contiguous()
                 n = int(np.asarray(m["xyz"]).shape[0]) if not torch.is_tensor(m["xyz"]) else m["xyz"].shape[0]
-                rot = t(m["rot"])
-                rot = rot / rot.norm(dim=1, keepdim=True)
-                pk = pack_map(t(m["xyz"]), t(m["opacity"]), t(m["sh"]), scales=t(m["scale"]), rotations=rot)
+                # rotations are taken as given: unit (w, x, y, z) quaternions, as the
+                # rasterizer receives them from GaussianModel.get_rotation
+                pk = pack_map(t(m["xyz"]), t(m["opacity"]), t(m["sh"]), scales=t(m["scale"]),
+                              rotations=t(m["rot"]))
             self.packed.append(pk)
             specs.append(MapSpec(n, packed=pk, sh_degree=3))
         views, pairs = [], []

@@ -342,13 +342,15 @@ static void frozen_fwd(int n, const pre_t_d *pre, const float *opac, int W, int 
     }
 }
 
-void or_frozen_render_f64(int n, const float *xyz, const float *scale, const float *rot,
-                          const float *cov_pre, double mod, const float *opac, const float *sh,
-                          int deg, const float *colors_pre, const double *view, int W, int H,
-                          int nch, const double *bg, const int64_t *rec_start,
-                          const uint32_t *rec_ids, const uint8_t *rec_clamp, double *out,
-                          double *out_depth, double *out_alpha)
+int or_frozen_render_f64(int n, const float *xyz, const float *scale, const float *rot,
+                         const float *cov_pre, double mod, const float *opac, const float *sh,
+                         int deg, const float *colors_pre, const double *view, int W, int H,
+                         int nch, const double *bg, const int64_t *rec_start,
+                         const uint32_t *rec_ids, const uint8_t *rec_clamp, double *out,
+                         double *out_depth, double *out_alpha)
 {
+    if (!cov_pre && (!scale || !rot)) return -1;
+    if (!sh && !colors_pre) return -1;
     double *cov6d = (double *)malloc(sizeof(double) * 6 * (size_t)(n > 0 ? n : 1));
     pre_t_d *pre = (pre_t_d *)malloc(sizeof(pre_t_d) * (size_t)(n > 0 ? n : 1));
     int *vis = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
@@ -358,6 +360,7 @@ void or_frozen_render_f64(int n, const float *xyz, const float *scale, const flo
     free(cov6d);
     free(pre);
     free(vis);
+    return 0;
 }
 
 /* SH basis values Y_k(dir) and their gradients d/d(x,y,z) (treating x,y,z as free) */
@@ -417,6 +420,10 @@ void or_frozen_backward_f64(int n, const float *xyz, const float *scale, const f
                             double *g_opac, double *g_scale, double *g_rot, double *g_cov,
                             double *g_colors)
 {
+    if ((!cov_pre && (!scale || !rot)) || (!sh && !colors_pre)) {
+        for (int k = 0; k < 6; ++k) g_xi[k] = NAN;
+        return;
+    }
     int P = W * H;
     size_t nn = (size_t)(n > 0 ? n : 1);
     double *cov6d = (double *)malloc(sizeof(double) * 6 * nn);

@@ -57,6 +57,7 @@ def lib():
                                    _opt(f32p), f32p, f32p, _opt(f32p), _opt(f32p), _opt(f32p),
                                    _opt(i32p), _opt(i32p), _opt(i32p), _opt(i64p), _opt(u32p),
                                    _opt(u8p)]
+        L.or_frozen_render_f64.restype = C.c_int
         L.or_frozen_render_f64.argtypes = [C.c_int, f32p, _opt(f32p), _opt(f32p), _opt(f32p),
                                            C.c_double, f32p, _opt(f32p), C.c_int, _opt(f32p), f64p,
                                            C.c_int, C.c_int, C.c_int, f64p, i64p, u32p, u8p, f64p,
@@ -167,7 +168,9 @@ def blend(W, H, rng, vals, pre, opac, colors, bg, record=False, want_extra=True)
         tot = int(start[-1])
         ids = np.zeros(max(tot, 1), np.uint32)
         clamp = np.zeros(max(tot, 1), np.uint8)
-        L.or_blend_fwd(*args, cnt, start, ids, clamp)
+        # second pass only records contributors: do not count n_touched twice
+        args2 = args[:-1] + (None,)
+        L.or_blend_fwd(*args2, cnt, start, ids, clamp)
         res.update(rec_start=start, rec_ids=ids, rec_clamp=clamp)
     return res
 
@@ -196,6 +199,8 @@ def frozen_render(rec, xyz, opac, view64, W, H, bg, nch, sh=None, scale=None, ro
     A = np.zeros((H, W), np.float64)
     bgv = np.zeros(3, np.float64)
     bgv[:len(bg)] = bg
+    if cov_pre is None and (scale is None or rot is None):
+        raise ValueError("frozen_render needs cov_pre or scale + rot")
     lib().or_frozen_render_f64(n, _c(xyz, np.float32), _c(scale, np.float32), _c(rot, np.float32),
                                _c(cov_pre, np.float32), mod, _c(opac, np.float32), _c(sh, np.float32),
                                sh_deg, _c(colors_pre, np.float32), _c(view64, np.float64), W, H, nch,

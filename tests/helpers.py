@@ -50,6 +50,7 @@ def oracle_pair_loss_f64(m, cam, R, t, lin, ang, dtau, E, recs, unsigned=False, 
     for (Rv, tv), rec in zip(((Rl, tl), (Rn, tn)), recs):
         v = view_vector(Rv, tv, cam, np.float64)
         out, _, _ = oracle.frozen_render(rec, m["xyz"], m["opacity"], v, cam.width, cam.height, [0.0], 1,
-                                         sh=m["sh"], cov_pre=cov)
+                                         sh=m["sh"], cov_pre=cov, scale=None if cov is not None else m["scale"],
+                                         rot=None if cov is not None else m["rot"])
         imgs.append(out[0])
     return oracle.loss_f64(imgs[0], imgs[1], E, unsigned)
