@@ -7,12 +7,8 @@
 int gs_launch_preprocess_fwd(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
 int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gsevt_map_grads *grads_dev,
                              double *xi_out, cudaStream_t s);
-int gs_launch_scan(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
-int gs_launch_duplicate(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
-int gs_launch_ranges(const gsevt_frame *f, const Workspace &ws, const unsigned long long *sorted_keys,
-                     uint32_t max_keys, cudaStream_t s);
-int gs_launch_sort(const gsevt_frame *f, const Workspace &ws, int bits, uint32_t max_keys, int *out_buf,
-                   cudaStream_t s);
+int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
+int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, cudaStream_t s);
 int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s);
 int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, const float *dL_dimage,
                         const float *dL_ddepth, const float *dL_dalpha, cudaStream_t s);
@@ -40,7 +36,7 @@ int check_frame(const gsevt_frame *f, Workspace *ws)
     return GSEVT_OK;
 }
 
-int sorted_buffer(const gsevt_frame *f) { return ((f->L.sort_bits + 7) / 8) & 1; }
+int sorted_buffer(const gsevt_frame *f) { return gs_tile_sort_buffer(f->L); }
 
 }  // namespace
 
@@ -57,7 +53,7 @@ extern "C" int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream)
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
     cudaMemsetAsync(ws.status, 0, 64, s);
-    cudaMemsetAsync(ws.sort_lookback, 0, (size_t)gs_sort_tiles(f->L.key_capacity > 0 ? f->L.key_capacity : 1) * 256 * 8, s);
+    cudaMemsetAsync(ws.sort_lookback, 0, (size_t)gs_lookback_tiles(f->L) * 256 * 8, s);
     if (f->L.num_pairs > 0) cudaMemsetAsync(ws.loss_done, 0, (size_t)f->L.num_pairs * 4, s);
     GS_CUDA_CHECK();
     return GSEVT_OK;
@@ -75,17 +71,19 @@ extern "C" void gsevt_abi_sizes(int32_t *out7)
     out7[6] = (int32_t)sizeof(gsevt_pose_state);
 }
 
-extern "C" void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out23)
+extern "C" void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out)
 {
-    if (!L || !out23) return;
+    if (!L || !out) return;
     // carve against a fake non-null base so absent regions stay null
     char *base = (char *)(uintptr_t)4096;
     Workspace w = gs_carve(*L, base);
-    const void *ptrs[23] = {w.status, w.bin, w.recA, w.recB, w.recC, w.gradA, w.gradB, w.gradC, w.scan_sums,
-                            w.scan_offs, w.keys[0], w.keys[1], w.vals[0], w.vals[1], w.sort_hist, w.sort_counter,
-                            w.sort_lookback, w.ranges, w.loss_part, w.loss_scal, w.loss_done, w.xi_part, w.xi};
-    for (int i = 0; i < 23; ++i)
-        out23[i] = ptrs[i] ? (uint64_t)((const char *)ptrs[i] - base) : UINT64_MAX;
+    const void *ptrs[GS_WS_REGIONS] = {w.status, w.bin, w.recA, w.recB, w.recC, w.gradA, w.gradB, w.gradC,
+                                       w.vis_sums, w.vis_offs, w.dkeys[0], w.dkeys[1], w.dvals[0], w.dvals[1],
+                                       w.tsums, w.toffs, w.keys[0], w.keys[1], w.vals[0], w.vals[1], w.sort_hist,
+                                       w.sort_counter, w.sort_lookback, w.ranges, w.loss_part, w.loss_scal,
+                                       w.loss_done, w.xi_part, w.xi};
+    for (int i = 0; i < GS_WS_REGIONS; ++i)
+        out[i] = ptrs[i] ? (uint64_t)((const char *)ptrs[i] - base) : UINT64_MAX;
 }
 
 extern "C" int gsevt_clear_status(const gsevt_frame *f, gsevt_stream_t stream)
@@ -120,7 +118,7 @@ extern "C" int gsevt_preprocess_fwd(const gsevt_frame *f, gsevt_stream_t stream)
     GS_CUDA_CHECK();
     st = gs_launch_preprocess_fwd(f, ws, s);
     if (st) return st;
-    return gs_launch_scan(f, ws, s);
+    return gs_launch_depth_order(f, ws, s);
 }
 
 extern "C" int gsevt_bin_and_sort(const gsevt_frame *f, uint32_t max_keys, gsevt_stream_t stream)
@@ -130,13 +128,7 @@ extern "C" int gsevt_bin_and_sort(const gsevt_frame *f, uint32_t max_keys, gsevt
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
     if (max_keys == 0 || max_keys > f->L.key_capacity) max_keys = f->L.key_capacity;
-    st = gs_launch_duplicate(f, ws, s);
-    if (st) return st;
-    int buf = 0;
-    st = gs_launch_sort(f, ws, f->L.sort_bits, max_keys, &buf, s);
-    if (st) return st;
-    if (buf != sorted_buffer(f)) return GSEVT_ERR_ARG;
-    return gs_launch_ranges(f, ws, ws.keys[buf], max_keys, s);
+    return gs_launch_bin(f, ws, max_keys, s);
 }
 
 extern "C" int gsevt_blend_fwd(const gsevt_frame *f, gsevt_stream_t stream)

@@ -51,7 +51,8 @@ __host__ __device__ __forceinline__ float gs_expf(float x)
 
 // ------------------------------------------------------------ workspace ---------
 struct Workspace {
-    uint32_t *status;     // [0] status bits, [1] num keys, [2] sort epoch, [3] sorted buffer
+    uint32_t *status;     // [0] status bits, [1] num keys, [2] last sort epoch, [4] sort epoch base,
+                          // [5] number of visible (view, Gaussian) slots
     int4 *bin;            // [num_vg] {touched, rect lo (x0 | y0<<16), rect hi, depth bits}
     float4 *recA;         // [num_vg] {mean x, mean y, depth, grey}
     float4 *recB;         // [num_vg] {conic x, y, z, opacity}
@@ -59,13 +60,17 @@ struct Workspace {
     float4 *gradA;        // [num_vg] dL/d{mean x, mean y, conic x, conic y}
     float4 *gradB;        // [num_vg] dL/d{conic z, opacity, grey or r, depth}
     float4 *gradC;        // [num_vg] dL/d{g, b, -, -} (channels == 3)
-    uint32_t *scan_sums;  // [num_scan_blocks]
-    uint32_t *scan_offs;  // [num_scan_blocks]
-    unsigned long long *keys[2];
-    uint32_t *vals[2];
+    uint32_t *vis_sums;   // [num_scan_blocks] visible slots per (view, block)
+    uint32_t *vis_offs;   // [num_scan_blocks]
+    uint32_t *dkeys[2];   // [num_vg] depth bits of the visible slots (depth sort)
+    uint32_t *dvals[2];   // [num_vg] their (view, Gaussian) slots
+    uint32_t *tsums;      // [sorted blocks] touched tiles per block of depth-sorted slots
+    uint32_t *toffs;      // [sorted blocks]
+    uint32_t *keys[2];    // [key_capacity] global tile id of each (tile, Gaussian) pair
+    uint32_t *vals[2];    // [key_capacity] its (view, Gaussian) slot
     uint32_t *sort_hist;      // [GS_MAX_PASSES][256]
     uint32_t *sort_counter;   // [GS_MAX_PASSES]
-    unsigned long long *sort_lookback;  // [max sort tiles][256]  {epoch:32 | flag:2 | count:30}
+    unsigned long long *sort_lookback;  // [sort tiles][256]  {epoch:32 | flag:2 | count:30}
     uint2 *ranges;        // [total_tiles]
     double *loss_part;    // [loss_blocks][4]
     double *loss_scal;    // [num_pairs][4] {s, cross, e2, L}
@@ -75,9 +80,20 @@ struct Workspace {
     size_t bytes;
 };
 
+#define GS_WS_REGIONS 29
+
 __host__ __device__ inline size_t gs_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
 inline uint32_t gs_sort_tiles(uint32_t cap) { return (cap + GS_SORT_TILE - 1) / GS_SORT_TILE; }
+inline uint32_t gs_sorted_blocks(const gsevt_layout &L) { return ((uint32_t)(L.num_vg > 0 ? L.num_vg : 1) + GS_BLOCK - 1) / GS_BLOCK; }
+inline uint32_t gs_lookback_tiles(const gsevt_layout &L)
+{
+    uint32_t cap = L.key_capacity > 0 ? L.key_capacity : 1;
+    uint32_t vg = L.num_vg > 0 ? (uint32_t)L.num_vg : 1;
+    return gs_sort_tiles(cap > vg ? cap : vg);
+}
+inline int gs_tile_bits(const gsevt_layout &L) { return L.sort_bits - 32; }
+inline int gs_tile_sort_buffer(const gsevt_layout &L) { return ((gs_tile_bits(L) + 7) / 8) & 1; }
 
 // Carves the workspace in a fixed order; with base == nullptr it only sizes it.
 inline Workspace gs_carve(const gsevt_layout &L, void *base)
@@ -100,16 +116,22 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     w.gradA = (float4 *)take(vg * 16);
     w.gradB = (float4 *)take(vg * 16);
     w.gradC = rgb ? (float4 *)take(vg * 16) : nullptr;
-    w.scan_sums = (uint32_t *)take((size_t)L.num_scan_blocks * 4);
-    w.scan_offs = (uint32_t *)take((size_t)L.num_scan_blocks * 4);
+    w.vis_sums = (uint32_t *)take((size_t)L.num_scan_blocks * 4);
+    w.vis_offs = (uint32_t *)take((size_t)L.num_scan_blocks * 4);
+    w.dkeys[0] = (uint32_t *)take(vg * 4);
+    w.dkeys[1] = (uint32_t *)take(vg * 4);
+    w.dvals[0] = (uint32_t *)take(vg * 4);
+    w.dvals[1] = (uint32_t *)take(vg * 4);
+    w.tsums = (uint32_t *)take((size_t)gs_sorted_blocks(L) * 4);
+    w.toffs = (uint32_t *)take((size_t)gs_sorted_blocks(L) * 4);
     size_t cap = (size_t)(L.key_capacity > 0 ? L.key_capacity : 1);
-    w.keys[0] = (unsigned long long *)take(cap * 8);
-    w.keys[1] = (unsigned long long *)take(cap * 8);
+    w.keys[0] = (uint32_t *)take(cap * 4);
+    w.keys[1] = (uint32_t *)take(cap * 4);
     w.vals[0] = (uint32_t *)take(cap * 4);
     w.vals[1] = (uint32_t *)take(cap * 4);
     w.sort_hist = (uint32_t *)take(GS_MAX_PASSES * 256 * 4);
     w.sort_counter = (uint32_t *)take(GS_MAX_PASSES * 4);
-    w.sort_lookback = (unsigned long long *)take((size_t)gs_sort_tiles((uint32_t)cap) * 256 * 8);
+    w.sort_lookback = (unsigned long long *)take((size_t)gs_lookback_tiles(L) * 256 * 8);
     w.ranges = (uint2 *)take((size_t)L.total_tiles * 8);
     w.loss_part = (double *)take((size_t)L.loss_blocks * 4 * 8);
     w.loss_scal = (double *)take((size_t)L.num_pairs * 4 * 8);

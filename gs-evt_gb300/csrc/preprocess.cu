@@ -4,7 +4,7 @@
 // of that map, so the 232 B of attributes (position, opacity, cov3D, 48 SH
 // coefficients) are read from HBM once per map and reused for all its views (the
 // (t, t+dtau) pair, or all pose hypotheses).  Per (view, Gaussian) slot it writes the
-// binning record, the two blend records and the per-view block sums for the key scan.
+// binning record, the two blend records and the per-(view, block) visible counts.
 // The arithmetic follows the oracle's FP32 instance (oracle/or_math.inc) operation by
 // operation: view transform, 1.3x guard-band Jacobian, EWA cov2D + 0.3, conic,
 // radius = ceil(3 sqrt(lambda_max)), 16x16 tile rect, SH degree-3 colour + 0.5 clamped
@@ -269,8 +269,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_preprocess_fwd(FwdParams p)
             }
             if (p.radii) p.radii[vg] = vis ? (int)fminf(o.radius, 1073741824.0f) : 0;
         }
-        // per (view, block) sum of touched tiles for the key scan
-        uint32_t s = touched;
+        // per (view, block) count of visible slots for the compaction scan
+        uint32_t s = touched > 0 ? 1u : 0u;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
         if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = s;
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_preprocess_fwd(FwdParams p)
         if (threadIdx.x == 0) {
             uint32_t tot = 0;
             for (int w = 0; w < GS_BLOCK / 32; ++w) tot += wsum[w];
-            p.ws.scan_sums[V.sb_offset + gb] = tot;
+            p.ws.vis_sums[V.sb_offset + gb] = tot;
         }
     }
 }

@@ -1,4 +1,4 @@
-// Onesweep LSD radix sort of (64-bit key, 32-bit value) pairs, 8-bit digits.
+// Onesweep LSD radix sort of (32- or 64-bit key, 32-bit value) pairs, 8-bit digits.
 //
 // Method: Adinets & Merrill, "Onesweep: A Faster Least Significant Digit Radix Sort
 // for GPUs" (2022).  One histogram kernel reads the keys once and counts the digits of
@@ -24,15 +24,15 @@ namespace {
 #define FLAG_AGG 1ull
 #define FLAG_PREFIX 2ull
 
-__global__ void k_sort_hist(const unsigned long long *keys, const uint32_t *status, uint32_t capacity,
-                            int passes, uint32_t *hist)
+template <typename KT>
+__global__ void k_sort_hist(const KT *keys, const uint32_t *count, uint32_t capacity, int passes, uint32_t *hist)
 {
     __shared__ uint32_t sh[GS_MAX_PASSES][256];
     for (int i = threadIdx.x; i < GS_MAX_PASSES * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
-    uint32_t K = min(status[1], capacity);
+    uint32_t K = min(*count, capacity);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
-        unsigned long long k = keys[i];
+        KT k = keys[i];
         for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(k >> (8 * p)) & 255], 1u);
     }
     __syncthreads();
@@ -50,22 +50,25 @@ __global__ void k_sort_epoch(uint32_t *status, int passes)
     status[2] = e + (uint32_t)passes;
 }
 
+template <typename KT>
 struct PassParams {
-    const unsigned long long *kin;
+    const KT *kin;
     const uint32_t *vin;
-    unsigned long long *kout;
+    KT *kout;
     uint32_t *vout;
     const uint32_t *hist;       // this pass's 256 digit counts
     uint32_t *counter;          // this pass's tile ticket counter
     unsigned long long *lookback;
     uint32_t *status;
+    const uint32_t *count;      // number of keys (device word)
     uint32_t capacity;
     int pass;
 };
 
-__global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams p)
+template <typename KT>
+__global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
 {
-    __shared__ unsigned long long skeys[SORT_TILE];
+    __shared__ KT skeys[SORT_TILE];
     __shared__ uint32_t svals[SORT_TILE];
     __shared__ uint32_t whist[GS_BLOCK / 32][256];
     __shared__ uint32_t dstart[256];
@@ -77,7 +80,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams p)
     if (tid == 0) s_tile = atomicAdd(p.counter, 1u);
     for (int i = tid; i < (GS_BLOCK / 32) * 256; i += GS_BLOCK) (&whist[0][0])[i] = 0;
     __syncthreads();
-    const uint32_t K = min(p.status[1], p.capacity);
+    const uint32_t K = min(*p.count, p.capacity);
     const uint32_t tile = s_tile;
     const uint32_t ntiles = (K + SORT_TILE - 1) / SORT_TILE;
     if (tile >= ntiles) return;
@@ -86,7 +89,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams p)
     const int shift = 8 * p.pass;
     const unsigned long long epoch = (unsigned long long)(p.status[4] + (uint32_t)p.pass);
 
-    unsigned long long key[SORT_KPT];
+    KT key[SORT_KPT];
     uint32_t val[SORT_KPT];
     uint32_t rank[SORT_KPT];
     int dig[SORT_KPT];
@@ -94,7 +97,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams p)
     for (int k = 0; k < SORT_KPT; ++k) {
         uint32_t li = (uint32_t)(w * 32 * SORT_KPT + k * 32 + lane);
         bool ok = li < count;
-        key[k] = ok ? p.kin[base + li] : 0ull;
+        key[k] = ok ? p.kin[base + li] : (KT)0;
         val[k] = ok ? p.vin[base + li] : 0u;
         dig[k] = ok ? (int)((key[k] >> shift) & 255) : 256;
     }
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams p)
     }
     __syncthreads();
     for (uint32_t i = tid; i < count; i += GS_BLOCK) {
-        unsigned long long kk = skeys[i];
+        KT kk = skeys[i];
         int dd = (int)((kk >> shift) & 255);
         uint32_t pos = gbase[dd] + (i - dstart[dd]);
         p.kout[pos] = kk;
@@ -185,41 +188,48 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams p)
 
 }  // namespace
 
-// Sorts ws.keys[0]/vals[0] (count in status[1]) on the low `bits` bits; the result is in
-// buffer index returned through *out_buf.  max_keys bounds the grid (host-known count, or
-// the capacity when the count is only known on the device).
-int gs_launch_sort(const gsevt_frame *f, const Workspace &ws, int bits, uint32_t max_keys, int *out_buf,
-                   cudaStream_t s)
+// Sorts keys[0]/vals[0] (count in *count, a device word) on the low `bits` bits; the
+// result is in buffer index (passes & 1), returned through *out_buf.  max_keys bounds
+// the grid (a host-known count, or the capacity when the count is only known on the
+// device).  The look-back table must hold gs_sort_tiles(capacity) * 256 entries.
+template <typename KT>
+int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
+                     int bits, uint32_t max_keys, const Workspace &ws, int *out_buf, cudaStream_t s)
 {
     int passes = (bits + 7) / 8;
     if (passes < 1) passes = 1;
-    if (passes > GS_MAX_PASSES) return GSEVT_ERR_ARG;
+    if (passes > GS_MAX_PASSES || passes * 8 > (int)(8 * sizeof(KT)) + 7) return GSEVT_ERR_ARG;
     *out_buf = passes & 1;
-    if (max_keys > f->L.key_capacity) max_keys = f->L.key_capacity;
+    if (max_keys > capacity) max_keys = capacity;
     if (max_keys == 0) return GSEVT_OK;
     cudaMemsetAsync(ws.sort_hist, 0, GS_MAX_PASSES * 256 * 4, s);
     cudaMemsetAsync(ws.sort_counter, 0, GS_MAX_PASSES * 4, s);
     GS_CUDA_CHECK();
     int hblocks = (int)std::min<uint32_t>((max_keys + 1023) / 1024, 152u * 4u);
-    k_sort_hist<<<hblocks, 256, 0, s>>>(ws.keys[0], ws.status, f->L.key_capacity, passes, ws.sort_hist);
+    k_sort_hist<KT><<<hblocks, 256, 0, s>>>(keys[0], count, capacity, passes, ws.sort_hist);
     k_sort_epoch<<<1, 1, 0, s>>>(ws.status, passes);
     GS_CUDA_CHECK();
     uint32_t tiles = (max_keys + SORT_TILE - 1) / SORT_TILE;
     for (int pass = 0; pass < passes; ++pass) {
-        PassParams p;
+        PassParams<KT> p;
         int src = pass & 1;
-        p.kin = ws.keys[src];
-        p.vin = ws.vals[src];
-        p.kout = ws.keys[src ^ 1];
-        p.vout = ws.vals[src ^ 1];
+        p.kin = keys[src];
+        p.vin = vals[src];
+        p.kout = keys[src ^ 1];
+        p.vout = vals[src ^ 1];
         p.hist = ws.sort_hist + 256 * pass;
         p.counter = ws.sort_counter + pass;
         p.lookback = ws.sort_lookback;
         p.status = ws.status;
-        p.capacity = f->L.key_capacity;
+        p.count = count;
+        p.capacity = capacity;
         p.pass = pass;
-        k_sort_pass<<<tiles, GS_BLOCK, 0, s>>>(p);
+        k_sort_pass<KT><<<tiles, GS_BLOCK, 0, s>>>(p);
         GS_CUDA_CHECK();
     }
     return GSEVT_OK;
 }
+
+template int gs_launch_sort_t<uint32_t>(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_t *count,
+                                        uint32_t capacity, int bits, uint32_t max_keys, const Workspace &ws,
+                                        int *out_buf, cudaStream_t s);

@@ -143,13 +143,14 @@ EXPORTED = [
 ]
 
 
-WORKSPACE_REGIONS = ["status", "bin", "recA", "recB", "recC", "gradA", "gradB", "gradC", "scan_sums",
-                     "scan_offs", "keys0", "keys1", "vals0", "vals1", "sort_hist", "sort_counter",
-                     "sort_lookback", "ranges", "loss_part", "loss_scal", "loss_done", "xi_part", "xi"]
+WORKSPACE_REGIONS = ["status", "bin", "recA", "recB", "recC", "gradA", "gradB", "gradC", "vis_sums",
+                     "vis_offs", "dkeys0", "dkeys1", "dvals0", "dvals1", "tsums", "toffs", "keys0", "keys1",
+                     "vals0", "vals1", "sort_hist", "sort_counter", "sort_lookback", "ranges", "loss_part",
+                     "loss_scal", "loss_done", "xi_part", "xi"]
 
 
 def workspace_offsets(layout):
-    out = (C.c_uint64 * 23)()
+    out = (C.c_uint64 * len(WORKSPACE_REGIONS))()
     lib().gsevt_workspace_offsets(C.byref(layout), out)
     return {k: (None if o == 0xFFFFFFFFFFFFFFFF else int(o)) for k, o in zip(WORKSPACE_REGIONS, out)}
 

@@ -159,11 +159,12 @@ int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream);
  * frame, pose_state (7 entries).  Touches no GPU state. */
 void gsevt_abi_sizes(int32_t *out7);
 /* Byte offsets of the workspace regions for a layout (introspection for tests and
- * tools), in this order: status, bin, recA, recB, recC, gradA, gradB, gradC,
- * scan_sums, scan_offs, keys0, keys1, vals0, vals1, sort_hist, sort_counter,
- * sort_lookback, ranges, loss_part, loss_scal, loss_done, xi_part, xi (23 entries;
- * absent regions are reported as UINT64_MAX).  Touches no GPU state. */
-void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out23);
+ * tools), in this order: status, bin, recA, recB, recC, gradA, gradB, gradC, vis_sums,
+ * vis_offs, dkeys0, dkeys1, dvals0, dvals1, tsums, toffs, keys0, keys1, vals0, vals1,
+ * sort_hist, sort_counter, sort_lookback, ranges, loss_part, loss_scal, loss_done,
+ * xi_part, xi (29 entries; absent regions are reported as UINT64_MAX).  keys are 32-bit
+ * global tile ids, vals 32-bit (view, Gaussian) slots.  Touches no GPU state. */
+void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out29);
 
 /* ---- map packing ----
  * Replaces the per-call activation + torch.cat of get_features
@@ -177,7 +178,8 @@ int gsevt_pack_map(int32_t n, const float *xyz, const float *opacity, const floa
  * preprocess: per (view, Gaussian) projection, EWA conic, radius, tile rect, SH colour.
  * Also writes radii (the forward's 2nd return value) when frame->radii is set. */
 int gsevt_preprocess_fwd(const gsevt_frame *f, gsevt_stream_t stream);
-/* key duplication, onesweep radix sort of (view|tile|depth) keys, tile ranges.
+/* key duplication in depth order, onesweep radix sort by (view|tile), tile ranges: the
+ * order of a stable sort of (view|tile|depth) keys.
  * max_keys bounds the sort grid: the host-known key count (after gsevt_read_status),
  * or 0 to size it from the key capacity (no host sync; CUDA-graph friendly). */
 int gsevt_bin_and_sort(const gsevt_frame *f, uint32_t max_keys, gsevt_stream_t stream);

@@ -94,10 +94,12 @@ def test_single_view_bit_exact(small, packed):
     # keys, sort order, ranges
     K = fr.num_keys
     assert K == res["keys"].shape[0]
-    buf = ((fr.L.sort_bits + 7) // 8) & 1
-    keys = _region(fr, "keys%d" % buf, torch.int64, K).cpu().numpy().view(np.uint64)
+    buf = ((fr.L.sort_bits - 32 + 7) // 8) & 1
+    tiles = _region(fr, "keys%d" % buf, torch.int32, K).cpu().numpy().view(np.uint32)
     vals = _region(fr, "vals%d" % buf, torch.int32, K).cpu().numpy().view(np.uint32)
-    assert np.array_equal(keys, res["keys"]) and np.array_equal(vals, res["vals"])
+    # same order as the stable sort of the full (tile | depth) keys, ties included
+    assert np.array_equal(tiles, (res["keys"] >> np.uint64(32)).astype(np.uint32))
+    assert np.array_equal(vals, res["vals"])
     rng = _region(fr, "ranges", torch.int32, 2 * fr.L.total_tiles).view(-1, 2).cpu().numpy().view(np.uint32)
     assert np.array_equal(rng, res["ranges"])
     # blend outputs

@@ -41,7 +41,7 @@ def test_workspace_sizing_and_offsets():
     small = _lib.lib().gsevt_workspace_bytes(C.byref(L))
     L.key_capacity = 200000
     big = _lib.lib().gsevt_workspace_bytes(C.byref(L))
-    assert big > small + 100000 * 24
+    assert big >= small + 100000 * 16  # two key and two value buffers of 4 bytes
     off = _lib.workspace_offsets(L)
     assert off["status"] == 0 and off["recC"] is None and off["gradC"] is None
     seen = [v for v in off.values() if v is not None]
