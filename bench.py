@@ -188,20 +188,23 @@ def algorithmic_bytes(bt, prob):
     binv = fr.workspace[off:off + 16 * fr.L.num_vg].view(torch.int32).view(-1, 4)
     nvis = int((binv[:, 0] > 0).sum().item())
     P = fr.L.total_pixels
-    passes = (fr.L.sort_bits + 7) // 8
+    passes = (fr.L.sort_bits - 32 + 7) // 8  # tile-sort passes over the pairs
     maps = len(fr.maps)
     return {
-        # attributes once per map (232 B), per (view, Gaussian) 16 B bin record, 32 B blend record
-        "preprocess_fwd": 232 * n * maps + 16 * n * V + 32 * nvis,
-        # read bin 16 B/slot, write 12 B/key; each pass reads and writes 12 B/key; histogram reads 8 B/key
-        "bin_and_sort": 16 * n * V + 12 * K + 24 * K * passes + 8 * K + 16 * K,
+        # attributes once per map (232 B), per (view, Gaussian) 16 B bin record, 32 B blend
+        # record; compaction + 4 depth-sort passes over the visible slots (8 B each way)
+        "preprocess_fwd": 232 * n * maps + 16 * n * V + 32 * nvis + 16 * nvis * 5,
+        # duplication: bin 16 B per visible slot, 8 B per pair written; each tile-sort pass
+        # reads and writes 8 B per pair; histogram 4 B per pair; ranges 8 B per pair
+        "bin_and_sort": 16 * nvis + 8 * K + 16 * K * passes + 4 * K + 8 * K,
         # per key: 4 B value + 32 B record gather; per pixel 8 B written
         "blend_fwd": 36 * K + 8 * P,
         "loss": 12 * P,
         # gather as forward, per pixel 12 B read, per visible slot 32 B gradient accumulation
         "blend_bwd": 36 * K + 12 * P + 32 * nvis,
         "preprocess_bwd": 232 * n * maps + 16 * n * V + 32 * nvis,
-        "counts": {"keys": K, "visible_slots": nvis, "pixels": P, "views": V, "sort_passes": passes},
+        "counts": {"keys": K, "visible_slots": nvis, "pixels": P, "views": V, "tile_sort_passes": passes,
+                   "depth_sort_passes": 4},
     }
 
 
@@ -460,8 +463,11 @@ def main():
             traffic = json.load(open(tpath)).get(args.workload, {}).get(top)
         except Exception:
             traffic = None
-    passes = (bt.frame.L.sort_bits + 7) // 8
-    launches_per_iter = 12 + passes
+    # kernels per iteration: preprocess, 2 scans, compaction, depth sort (hist, epoch, 4 passes),
+    # sorted sums, duplication, tile sort (hist, epoch, passes), ranges, blend fwd, loss,
+    # blend bwd, preprocess bwd, twist reduction, finalize
+    tile_passes = (bt.frame.L.sort_bits - 32 + 7) // 8
+    launches_per_iter = 21 + tile_passes
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -192,9 +192,41 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
 //   0,1 mean x,y (pixels)  2,3,4 conic x,y,z  5 opacity  6 colour (grey or r)  7 depth
 //   8,9 colour g,b (RGB only).
 // Modes: 0 tracker (grey, pose only: 0-4 and 6), 1 grey drop-in (0-7), 2 RGB drop-in (0-9).
-template <int MODE> struct Comps { static constexpr int n = MODE == 0 ? 6 : (MODE == 1 ? 8 : 10); };
+template <int MODE> struct Comps {
+    static constexpr int n = MODE == 0 ? 6 : (MODE == 1 ? 8 : 10);
+    static constexpr int padded = MODE == 2 ? 16 : 8;  // power of two for the transposed reduction
+};
 template <int MODE>
 __device__ __forceinline__ constexpr int comp_idx(int q) { return (MODE == 0 && q >= 5) ? 6 : q; }
+
+// Transposed butterfly: reduces NV values (a power of two, 8 or 16) over the warp with
+// NV - 1 + (5 - log2 NV) shuffles instead of 5 per value.  At each halving stage a lane
+// keeps one half of its values and trades the other half with its partner; afterwards
+// lane l holds the warp total of component (l >> (5 - log2 NV)) & (NV - 1).
+template <int NV>
+__device__ __forceinline__ float warp_reduce_transposed(float (&v)[NV], int lane)
+{
+    int m = NV;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        if (m > 1) {
+            const bool hi = (lane & o) != 0;
+            const int half = m >> 1;
+#pragma unroll
+            for (int k = 0; k < NV / 2; ++k) {
+                if (k < half) {
+                    const float send = hi ? v[k] : v[half + k];
+                    const float keep = hi ? v[half + k] : v[k];
+                    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+                }
+            }
+            m = half;
+        } else {
+            v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+        }
+    }
+    return v[0];
+}
 
 template <int MODE>
 __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
@@ -342,11 +374,14 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                     }
                 }
                 if (__any_sync(0xffffffffu, contrib)) {
+                    constexpr int NV = Comps<MODE>::padded;
+                    constexpr int SH = NV == 8 ? 2 : 1;  // 5 - log2(NV)
+                    float red[NV];
 #pragma unroll
-                    for (int q = 0; q < NC; ++q) {
-                        const float s = warp_sum(gv[comp_idx<MODE>(q)]);
-                        if (lane == 0 && s != 0.0f) atomicAdd(&acc[j][q], s);
-                    }
+                    for (int q = 0; q < NV; ++q) red[q] = q < NC ? gv[comp_idx<MODE>(q)] : 0.0f;
+                    const float s = warp_reduce_transposed<NV>(red, lane);
+                    const int q = (lane >> SH) & (NV - 1);
+                    if ((lane & ((1 << SH) - 1)) == 0 && q < NC && s != 0.0f) atomicAdd(&acc[j][q], s);
                 }
             }
         }
