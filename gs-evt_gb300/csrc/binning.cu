@@ -137,12 +137,17 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sorted_sums(BinParams p, const uin
     }
 }
 
+// Warp-cooperative duplication: each warp expands the pairs of its 32 depth-sorted slots
+// into one contiguous output range, lane k writing pair k, k + 32, ... of that range
+// (coalesced); the owning slot of a pair is found by a shuffle binary search over the
+// warp's exclusive prefix of tile counts.
 __global__ void __launch_bounds__(GS_BLOCK) k_duplicate(BinParams p, const uint32_t *sorted_vals)
 {
     __shared__ uint32_t wtot[GS_BLOCK / 32];
     const uint32_t nvis = p.ws.status[5];
     const uint32_t i = blockIdx.x * GS_BLOCK + threadIdx.x;
     if (blockIdx.x * GS_BLOCK >= nvis) return;  // uniform per block
+    const int lane = threadIdx.x & 31;
     uint32_t vg = 0;
     int4 bin = make_int4(0, 0, 0, 0);
     if (i < nvis) {
@@ -151,22 +156,49 @@ __global__ void __launch_bounds__(GS_BLOCK) k_duplicate(BinParams p, const uint3
     }
     const uint32_t cnt = (uint32_t)bin.x;
     const uint32_t off = p.ws.toffs[blockIdx.x] + block_excl_scan(cnt, wtot);
-    if (cnt == 0) return;
-    p.ws.gradA[vg] = make_float4(0, 0, 0, 0);
-    p.ws.gradB[vg] = make_float4(0, 0, 0, 0);
-    if (p.rgb) p.ws.gradC[vg] = make_float4(0, 0, 0, 0);
-    const gsevt_view &V = p.views[find_view_by_vg(p.views, p.num_views, vg)];
-    const int x0 = bin.y & 0xffff, y0 = (bin.y >> 16) & 0xffff;
-    const int x1 = bin.z & 0xffff, y1 = (bin.z >> 16) & 0xffff;
-    uint32_t k = off;
-    for (int y = y0; y < y1; ++y)
-        for (int x = x0; x < x1; ++x) {
-            if (k < p.capacity) {
-                p.ws.keys[0][k] = (uint32_t)(V.tile_offset + y * V.tiles_x + x);
-                p.ws.vals[0][k] = vg;
-            }
-            ++k;
+    int x0 = 0, y0 = 0, rw = 1, toff = 0, tpx = 1;
+    if (cnt > 0) {
+        p.ws.gradA[vg] = make_float4(0, 0, 0, 0);
+        p.ws.gradB[vg] = make_float4(0, 0, 0, 0);
+        if (p.rgb) p.ws.gradC[vg] = make_float4(0, 0, 0, 0);
+        const gsevt_view &V = p.views[find_view_by_vg(p.views, p.num_views, vg)];
+        x0 = bin.y & 0xffff;
+        y0 = (bin.y >> 16) & 0xffff;
+        rw = (bin.z & 0xffff) - x0;
+        toff = V.tile_offset;
+        tpx = V.tiles_x;
+    }
+    // warp-level exclusive prefix of the counts and the warp's output base
+    uint32_t winc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, winc, o);
+        if (lane >= o) winc += y;
+    }
+    const uint32_t wex = winc - cnt;
+    const uint32_t wtotal = __shfl_sync(0xffffffffu, winc, 31);
+    const uint32_t wbase = __shfl_sync(0xffffffffu, off, 0);
+    for (uint32_t c = 0; c < wtotal; c += 32) {
+        const uint32_t k = c + lane;
+        // owner: the largest lane s with wex_s <= k (empty slots resolve to a later lane)
+        int s = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t e = __shfl_sync(0xffffffffu, wex, s + step);
+            if (e <= k) s += step;
         }
+        const uint32_t q = k - __shfl_sync(0xffffffffu, wex, s);
+        const int sx0 = __shfl_sync(0xffffffffu, x0, s), sy0 = __shfl_sync(0xffffffffu, y0, s);
+        const int srw = __shfl_sync(0xffffffffu, rw, s), stoff = __shfl_sync(0xffffffffu, toff, s);
+        const int stpx = __shfl_sync(0xffffffffu, tpx, s);
+        const uint32_t svg = __shfl_sync(0xffffffffu, vg, s);
+        const uint32_t idx = wbase + k;
+        if (k < wtotal && idx < p.capacity) {
+            const int y = sy0 + (int)(q / (uint32_t)srw), x = sx0 + (int)(q % (uint32_t)srw);
+            p.ws.keys[0][idx] = (uint32_t)(stoff + y * stpx + x);
+            p.ws.vals[0][idx] = svg;
+        }
+    }
 }
 
 __global__ void k_ranges(const uint32_t *keys, const uint32_t *status, uint32_t capacity, uint2 *ranges)

@@ -54,6 +54,7 @@ struct Batch {
     float4 B[GS_BLOCK];
     float4 C[GS_BLOCK];
     float4 box[GS_BLOCK];  // {xmin, xmax, ymin, ymax}: outside it the Gaussian fails the alpha test
+    float thr[GS_BLOCK];   // power below this value cannot pass the alpha test
     uint32_t id[GS_BLOCK];
 };
 
@@ -65,11 +66,16 @@ struct Batch {
 // 2 ulp and logf).  The box of that ellipse, widened by 0.1 % + 0.5 px, therefore never
 // excludes a pixel whose per-pixel test would pass, so culling against it leaves every
 // blending decision - and the result bits - unchanged.
-__device__ __forceinline__ float4 gauss_box(float4 A, float4 B)
+// Also returns, through *thr, a power threshold: below -(ln(255 o) (1 + 1e-4) + 1e-3),
+// o exp(power) < 0.999 / 255, so alpha < 1/255 whatever exp's last bits - the exp and the
+// alpha test can be skipped there without changing any decision.
+__device__ __forceinline__ float4 gauss_box(float4 A, float4 B, float *thr)
 {
     const float o = B.w;
+    *thr = 1e30f;
     if (!(o >= (1.0f / 255.0f) * 0.999f)) return make_float4(1e30f, -1e30f, 1e30f, -1e30f);
     const float tau = logf(255.0f * o) * 1.0001f + 1e-3f;
+    *thr = -tau;
     const float g = 1e-6f * (fabsf(B.x) + fabsf(B.z));
     const float a = 0.5f * B.x - g, b = 0.5f * B.y, c = 0.5f * B.z - g;
     const float det = a * c - b * b;
@@ -127,7 +133,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
         }
         if (__syncthreads_count(done) == GS_BLOCK) break;
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
-        if ((int)threadIdx.x < n) cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x]);
+        if ((int)threadIdx.x < n)
+            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &cur.thr[threadIdx.x]);
         __syncthreads();
         bool warp_done = false;
         for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
@@ -146,8 +153,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
                 const float4 A = cur.A[j], B = cur.B[j];
                 const float dx = A.x - pxf, dy = A.y - pyf;
                 const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
-                // power > 0, or exp(-5.6) * 1 < 1/255 (fails the alpha test anyway): skip
-                if (power > 0.0f || (power < -5.6f && B.w <= 1.0f)) continue;
+                // power > 0, or below the Gaussian's alpha threshold (fails the alpha test anyway)
+                if (power > 0.0f || power < cur.thr[j]) continue;
                 const float alpha = fminf(0.99f, B.w * gs_expf(power));
                 if (alpha < 1.0f / 255.0f) continue;
                 const float test_T = T * (1.0f - alpha);
@@ -306,7 +313,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         }
         if (__syncthreads_count(done) == GS_BLOCK) break;
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
-        if ((int)threadIdx.x < n) cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x]);
+        if ((int)threadIdx.x < n)
+            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &cur.thr[threadIdx.x]);
         __syncthreads();
         bool warp_done = false;
         for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
@@ -328,7 +336,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                     const float4 A = cur.A[j], B = cur.B[j];
                     const float dx = A.x - pxf, dy = A.y - pyf;
                     const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
-                    if (power <= 0.0f && !(power < -5.6f && B.w <= 1.0f)) {
+                    if (power <= 0.0f && !(power < cur.thr[j])) {
                         const float G = gs_expf(power);
                         const float araw = B.w * G;
                         const float alpha = fminf(0.99f, araw);

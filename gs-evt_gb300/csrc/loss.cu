@@ -5,7 +5,8 @@
 // ~8 forward and ~10 backward torch kernels per iteration.  With s = ||dI||,
 // c = sum(dI E) (signed) or sum(|dI| |E|) (unsigned) and e2 = sum(E^2),
 //   L^2 = 1 - 2 c / s + e2,
-// so one FP64 reduction pass gives L; the per-pixel gradient
+// so one reduction pass gives L (FP32 over each thread's 8 pixels, FP64 from the warp
+// level up); the per-pixel gradient
 //   dL/dI_next = -dL/dI_last = (g - n (n.g)) / s,  n.g = (1 - c/s) / L,
 // is formed inside the blend adjoint from (s, c, L) without another pass.
 // Each block reduces a slice of one pair into FP64 partials; the last block of the
@@ -39,31 +40,31 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     const gsevt_view &Vn = views[pr.next_view];
     const int P = Vl.width * Vl.height;
     const int lb = b - pr.block_offset;
-    double s2 = 0.0, cr = 0.0, e2 = 0.0;
+    // FP32 sums over this thread's 8 pixels, FP64 from the warp level up
+    float s2 = 0.0f, cr = 0.0f, e2 = 0.0f;
     const int base = lb * GS_BLOCK * LOSS_PIX_PER_THREAD;
+#pragma unroll
     for (int k = 0; k < LOSS_PIX_PER_THREAD; ++k) {
         int i = base + k * GS_BLOCK + threadIdx.x;
         if (i < P) {
             float d = image[Vn.pix_offset + i] - image[Vl.pix_offset + i];
-            float e = pr.event[i];
-            s2 += (double)d * (double)d;
-            e2 += (double)e * (double)e;
-            cr += pr.unsigned_mode ? (double)fabsf(d) * (double)fabsf(e) : (double)d * (double)e;
+            float e = __ldg(pr.event + i);
+            s2 = fmaf(d, d, s2);
+            e2 = fmaf(e, e, e2);
+            cr = pr.unsigned_mode ? fmaf(fabsf(d), fabsf(e), cr) : fmaf(d, e, cr);
         }
     }
-    s2 = warp_sum_d(s2);
-    cr = warp_sum_d(cr);
-    e2 = warp_sum_d(e2);
+    double S2 = warp_sum_d((double)s2), CR = warp_sum_d((double)cr), E2 = warp_sum_d((double)e2);
     if ((threadIdx.x & 31) == 0) {
-        part[threadIdx.x >> 5][0] = s2;
-        part[threadIdx.x >> 5][1] = cr;
-        part[threadIdx.x >> 5][2] = e2;
+        part[threadIdx.x >> 5][0] = S2;
+        part[threadIdx.x >> 5][1] = CR;
+        part[threadIdx.x >> 5][2] = E2;
     }
     __syncthreads();
     if (threadIdx.x < 3) {
-        double s = 0.0;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) s += part[w][threadIdx.x];
-        ws.loss_part[(size_t)b * 4 + threadIdx.x] = s;
+        double t = 0.0;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) t += part[w][threadIdx.x];
+        ws.loss_part[(size_t)b * 4 + threadIdx.x] = t;
     }
     __threadfence();
     __syncthreads();
@@ -74,21 +75,35 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     __syncthreads();
     if (!is_last) return;
     __threadfence();
+    // the last block of the pair adds the block partials: each thread a strided subset in
+    // a fixed order, then a fixed-shape tree, so the result does not depend on scheduling
+    const volatile double *lp = ws.loss_part;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int i = threadIdx.x; i < pr.num_blocks; i += GS_BLOCK) {
+        size_t q = (size_t)(pr.block_offset + i) * 4;
+        a0 += lp[q];
+        a1 += lp[q + 1];
+        a2 += lp[q + 2];
+    }
+    a0 = warp_sum_d(a0);
+    a1 = warp_sum_d(a1);
+    a2 = warp_sum_d(a2);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        part[threadIdx.x >> 5][0] = a0;
+        part[threadIdx.x >> 5][1] = a1;
+        part[threadIdx.x >> 5][2] = a2;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        double S2 = 0, CR = 0, E2 = 0;
-        const volatile double *lp = ws.loss_part;
-        for (int i = 0; i < pr.num_blocks; ++i) {
-            size_t q = (size_t)(pr.block_offset + i) * 4;
-            S2 += lp[q];
-            CR += lp[q + 1];
-            E2 += lp[q + 2];
-        }
-        double s = sqrt(S2);
-        double L2 = 1.0 - 2.0 * CR / s + E2;
+        double S2t = 0, CRt = 0, E2t = 0;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) { S2t += part[w][0]; CRt += part[w][1]; E2t += part[w][2]; }
+        double s = sqrt(S2t);
+        double L2 = 1.0 - 2.0 * CRt / s + E2t;
         double L = sqrt(L2 > 0.0 ? L2 : 0.0);
         ws.loss_scal[4 * pi + 0] = s;
-        ws.loss_scal[4 * pi + 1] = CR;
-        ws.loss_scal[4 * pi + 2] = E2;
+        ws.loss_scal[4 * pi + 1] = CRt;
+        ws.loss_scal[4 * pi + 2] = E2t;
         ws.loss_scal[4 * pi + 3] = L;
         if (loss_out) loss_out[pi] = L;
         if (!(L == L) || !(s > 0.0)) atomicOr(ws.status, GSEVT_STATUS_NONFINITE);

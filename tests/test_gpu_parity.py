@@ -206,7 +206,7 @@ def test_pair_loss_and_twist_gradients(unsigned):
     for i in range(2):
         assert _bits_equal(fr.pixels(i)[0].cpu().numpy(), imgs[i])
     L_ref, gn, gl = oracle.loss(imgs[0], imgs[1], E, unsigned, grads=True)
-    assert abs(loss.item() - L_ref) <= 1e-10 * abs(L_ref)  # FP64 sums in a different order
+    assert abs(loss.item() - L_ref) <= 1e-6 * abs(L_ref)  # FP32 per-thread partials, FP64 above
     xi = xi.cpu().numpy()
     for i, ((Rv, tv), g) in enumerate(zip(views, (gl, gn))):
         g_ref, _ = oracle.frozen_backward(recs[i], m["xyz"], m["opacity"], helpers.view_vector(Rv, tv, cam, np.float64),
@@ -233,7 +233,7 @@ def test_twelve_vector_against_finite_differences():
         g_gpu = st["grad"][0]
         recs = [oracle.rasterize_view(m["xyz"], helpers.cov6(m), m["sh"], m["opacity"], table[i], cam.width,
                                       cam.height, [0.0], nch=1, record=True) for i in range(2)]
-        assert abs(st["loss"][0] - oracle.loss(recs[0]["image"][0], recs[1]["image"][0], E)) < 1e-9
+        assert abs(st["loss"][0] - oracle.loss(recs[0]["image"][0], recs[1]["image"][0], E)) < 1e-6
 
         def L(d):
             T = opose.se3_exp(np.concatenate([d[3:6], d[0:3]])) @ opose.pose_matrix(R, t)
