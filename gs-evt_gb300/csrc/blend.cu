@@ -100,6 +100,22 @@ __device__ __forceinline__ void load_batch(const BlendParams &p, Batch &buf, uin
     cp_async_commit();
 }
 
+// Pixel of thread t: warps tile the 16x16 tile as 2 x 4 blocks of 8x4 pixels, so a warp's
+// footprint is nearly square (fewer Gaussians overlap it than a 16x2 strip).
+__device__ __forceinline__ void warp_pixel(int tid, int tx, int ty, int &px, int &py, float &sx0, float &sx1,
+                                           float &sy0, float &sy1)
+{
+    const int w = tid >> 5, l = tid & 31;
+    const int bx = tx * GSEVT_TILE + (w & 1) * 8, by = ty * GSEVT_TILE + (w >> 1) * 4;
+    px = bx + (l & 7);
+    py = by + (l >> 3);
+    sx0 = (float)bx;
+    sx1 = (float)(bx + 7);
+    sy0 = (float)by;
+    sy1 = (float)(by + 3);
+}
+
+template <bool DEPTH>
 __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
 {
     __shared__ Batch sb[2];
@@ -109,7 +125,9 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
     __syncthreads();
     const int lt = tile - V.tile_offset;
     const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
-    const int px = tx * GSEVT_TILE + (threadIdx.x & 15), py = ty * GSEVT_TILE + (threadIdx.x >> 4);
+    int px, py;
+    float sx0, sx1, sy0, sy1;
+    warp_pixel(threadIdx.x, tx, ty, px, py, sx0, sx1, sy0, sy1);
     const bool inside = px < V.width && py < V.height;
     const float pxf = (float)px, pyf = (float)py;
     const uint2 range = p.ws.ranges[tile];
@@ -118,10 +136,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
     float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f, Aacc = 0.0f;
     int last = 0;
     bool done = !inside;
-    // this warp's pixel strip: full tile width, rows 2w and 2w + 1
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const float sx0 = (float)(tx * GSEVT_TILE), sx1 = sx0 + (float)(GSEVT_TILE - 1);
-    const float sy0 = (float)(ty * GSEVT_TILE + 2 * w), sy1 = sy0 + 1.0f;
+    const int lane = threadIdx.x & 31;
     if (rounds > 0) load_batch(p, sb[0], range, 0);
     for (int r = 0; r < rounds; ++r) {
         Batch &cur = sb[r & 1];
@@ -133,8 +148,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
         }
         if (__syncthreads_count(done) == GS_BLOCK) break;
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
-        if ((int)threadIdx.x < n)
-            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &cur.thr[threadIdx.x]);
+        if ((int)threadIdx.x < n) {
+            float th;
+            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &th);
+            if (DEPTH) cur.thr[threadIdx.x] = th;
+            else cur.A[threadIdx.x].z = th;  // depth is not needed: keep the threshold in its slot
+        }
         __syncthreads();
         bool warp_done = false;
         for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
@@ -154,7 +173,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
                 const float dx = A.x - pxf, dy = A.y - pyf;
                 const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
                 // power > 0, or below the Gaussian's alpha threshold (fails the alpha test anyway)
-                if (power > 0.0f || power < cur.thr[j]) continue;
+                if (power > 0.0f || power < (DEPTH ? cur.thr[j] : A.z)) continue;
                 const float alpha = fminf(0.99f, B.w * gs_expf(power));
                 if (alpha < 1.0f / 255.0f) continue;
                 const float test_T = T * (1.0f - alpha);
@@ -167,7 +186,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
                 } else {
                     C0 = C0 + (A.w * alpha) * T;
                 }
-                D = D + (A.z * alpha) * T;
+                if (DEPTH) D = D + (A.z * alpha) * T;
                 Aacc = Aacc + alpha * T;
                 if (p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
                 T = test_T;
@@ -247,14 +266,14 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
     if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
     for (int i = threadIdx.x; i < GS_BLOCK * (NC + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
     __syncthreads();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     const int lt = tile - V.tile_offset;
     const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
-    const int px = tx * GSEVT_TILE + (threadIdx.x & 15), py = ty * GSEVT_TILE + (threadIdx.x >> 4);
+    int px, py;
+    float sx0, sx1, sy0, sy1;
+    warp_pixel(threadIdx.x, tx, ty, px, py, sx0, sx1, sy0, sy1);
     const bool inside = px < V.width && py < V.height;
     const float pxf = (float)px, pyf = (float)py;
-    const float sx0 = (float)(tx * GSEVT_TILE), sx1 = sx0 + (float)(GSEVT_TILE - 1);
-    const float sy0 = (float)(ty * GSEVT_TILE + 2 * w), sy1 = sy0 + 1.0f;
     const uint2 range = p.ws.ranges[tile];
     const int todo = (int)(range.y - range.x);
     const int rounds = (todo + GS_BLOCK - 1) / GS_BLOCK;
@@ -313,8 +332,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         }
         if (__syncthreads_count(done) == GS_BLOCK) break;
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
-        if ((int)threadIdx.x < n)
-            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &cur.thr[threadIdx.x]);
+        if ((int)threadIdx.x < n) {
+            float th;
+            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &th);
+            if (MODE != 0) cur.thr[threadIdx.x] = th;
+            else cur.A[threadIdx.x].z = th;  // the tracker adjoint needs no depth
+        }
         __syncthreads();
         bool warp_done = false;
         for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
@@ -336,7 +359,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                     const float4 A = cur.A[j], B = cur.B[j];
                     const float dx = A.x - pxf, dy = A.y - pyf;
                     const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
-                    if (power <= 0.0f && !(power < cur.thr[j])) {
+                    if (power <= 0.0f && !(power < (MODE != 0 ? cur.thr[j] : A.z))) {
                         const float G = gs_expf(power);
                         const float araw = B.w * G;
                         const float alpha = fminf(0.99f, araw);
@@ -440,7 +463,8 @@ int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     if (f->L.total_tiles <= 0) return GSEVT_OK;
     BlendParams p = make_params(f, ws, vals);
     if (f->n_touched) cudaMemsetAsync(f->n_touched, 0, (size_t)f->L.num_vg * 4, s);
-    k_blend_fwd<<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    if (f->depth) k_blend_fwd<true><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    else k_blend_fwd<false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

@@ -379,7 +379,7 @@ __device__ __forceinline__ void sh_basis(int deg, float x, float y, float z, flo
 }
 
 template <bool MAPGRAD>
-__global__ void __launch_bounds__(GS_BLOCK) k_preprocess_bwd(BwdParams p)
+__global__ void __launch_bounds__(GS_BLOCK, MAPGRAD ? 1 : 2) k_preprocess_bwd(BwdParams p)
 {
     __shared__ gsevt_map M;
     __shared__ gsevt_view V;
