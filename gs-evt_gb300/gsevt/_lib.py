@@ -121,7 +121,8 @@ def lib():
         "gsevt_read_status": (C.c_int, [fp, C.POINTER(u32), vp]),
         "gsevt_clear_status": (C.c_int, [fp, vp]),
         "gsevt_event_scratch_bytes": (C.c_size_t, [i32, i32]),
-        "gsevt_events_accumulate": (C.c_int, [i64, vp, vp, vp, i32, i32, i32, i32, vp, vp, vp, vp]),
+        "gsevt_events_accumulate": (C.c_int, [i64, vp, vp, vp, i32, i32, C.POINTER(C.c_double), i32, i32, vp,
+                                              vp, vp, vp]),
         "gsevt_track_step_batched": (C.c_int, [fp, vp, i32, vp, vp]),
         "gsevt_track_init_views": (C.c_int, [vp, vp, i32, vp]),
     }

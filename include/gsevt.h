@@ -228,16 +228,18 @@ int gsevt_read_status(const gsevt_frame *f, uint32_t *out2, gsevt_stream_t strea
 int gsevt_clear_status(const gsevt_frame *f, gsevt_stream_t stream);
 
 /* ---- event frame (utils/event_camera/event.py:116-128, tracker.py:78-91) ----
- * count += +1/-1 per event (int32 atomics), separable ksize Gaussian blur
- * (sigma = 0.3((ksize-1)/2 - 1) + 0.8, replicate border), L2 normalisation,
- * |E|, and nearest-neighbour pyramid levels.  out_signed / out_unsigned hold the
- * levels back to back: level l is int(W*0.5^l) x int(H*0.5^l).  scratch must hold
- * gsevt_event_scratch_bytes(W, H). */
+ * count += +1/-1 per event (int32 atomics); when camera (host array {fx, fy, cx, cy,
+ * k1, k2, p1, p2, k3}) is non-NULL, undistortion as cv2.undistort with the camera matrix
+ * reused (source position rounded to 1/32 pixel, bilinear, zero border); separable ksize
+ * Gaussian blur (sigma = 0.3((ksize-1)/2 - 1) + 0.8, replicate border), L2
+ * normalisation, |E|, and nearest-neighbour pyramid levels.  out_signed / out_unsigned
+ * hold the levels back to back: level l is int(W*0.5^l) x int(H*0.5^l).  scratch must
+ * hold gsevt_event_scratch_bytes(W, H). */
 size_t gsevt_event_scratch_bytes(int32_t width, int32_t height);
 int gsevt_events_accumulate(int64_t n, const uint16_t *x, const uint16_t *y,
                             const uint8_t *polarity, int32_t width, int32_t height,
-                            int32_t ksize, int32_t levels, void *scratch, float *out_signed,
-                            float *out_unsigned, gsevt_stream_t stream);
+                            const double *camera, int32_t ksize, int32_t levels, void *scratch,
+                            float *out_signed, float *out_unsigned, gsevt_stream_t stream);
 
 /* ---- batched tracker iteration (utils/tracker.py:176-240) ----
  * Per pose state (one tracking hypothesis / sequence): FP64 pose, velocity, Adam

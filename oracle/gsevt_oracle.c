@@ -689,15 +689,49 @@ double or_loss(int64_t npix, const float *I_last, const float *I_next, const flo
 }
 
 /* --------------------------------------------------------------- events -- */
+/* Undistortion of a float image (cv2.undistort with the camera matrix reused as the new
+ * camera matrix, as utils/event_camera/event.py:121 calls it).  OpenCV's documented
+ * model: for destination pixel (u, v), x = (u - cx)/fx, y = (v - cy)/fy, r2 = x^2 + y^2,
+ * kr = 1 + ((k3 r2 + k2) r2 + k1) r2, xd = x kr + 2 p1 x y + p2 (r2 + 2 x^2),
+ * yd = y kr + p1 (r2 + 2 y^2) + 2 p2 x y, source = (fx xd + cx, fy yd + cy); the source
+ * position is rounded to 1/32 pixel (INTER_TAB_SIZE = 32) and sampled bilinearly with a
+ * zero border.  cam = {fx, fy, cx, cy, k1, k2, p1, p2, k3}. */
+void or_undistort(const float *src, int W, int H, const double *cam, float *dst)
+{
+    double fx = cam[0], fy = cam[1], cx = cam[2], cy = cam[3];
+    double k1 = cam[4], k2 = cam[5], p1 = cam[6], p2 = cam[7], k3 = cam[8];
+    for (int v = 0; v < H; ++v)
+        for (int u = 0; u < W; ++u) {
+            double x = (u - cx) / fx, y = (v - cy) / fy;
+            double x2 = x * x, y2 = y * y, r2 = x2 + y2, xy2 = 2.0 * x * y;
+            double kr = 1.0 + ((k3 * r2 + k2) * r2 + k1) * r2;
+            double xd = x * kr + p1 * xy2 + p2 * (r2 + 2.0 * x2);
+            double yd = y * kr + p1 * (r2 + 2.0 * y2) + p2 * xy2;
+            double mx = fx * xd + cx, my = fy * yd + cy;
+            long iu = lrint(mx * 32.0), iv = lrint(my * 32.0);
+            long ix = iu >> 5, iy = iv >> 5;
+            float ax = (float)(iu & 31) / 32.0f, ay = (float)(iv & 31) / 32.0f;
+            float acc = 0.0f;
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) {
+                    long sx = ix + dx, sy = iy + dy;
+                    if (sx < 0 || sy < 0 || sx >= W || sy >= H) continue;
+                    float w = (dx ? ax : 1.0f - ax) * (dy ? ay : 1.0f - ay);
+                    acc += w * src[(size_t)sy * W + sx];
+                }
+            dst[(size_t)v * W + u] = acc;
+        }
+}
+
 /* Event frame (utils/event_camera/event.py:116-128): count[y][x] += +1/-1 per event
- * (EVENT_BRIGHTNESS = 1, event.py:8), undistortion is the identity for zero distortion
- * (not applied here), separable Gaussian blur with the OpenCV kernel of size ksize and
+ * (EVENT_BRIGHTNESS = 1, event.py:8), undistortion when cam is given (or_undistort),
+ * separable Gaussian blur with the OpenCV kernel of size ksize and
  * sigma = 0.3*((ksize-1)*0.5 - 1) + 0.8 with BORDER_REPLICATE, then division by the
  * L2 norm (cv2.normalize defaults: NORM_L2, alpha 1; zero frame stays zero).
  * Blur arithmetic in double, results rounded to float. */
 void or_event_frame(int W, int H, int64_t n, const uint16_t *ex, const uint16_t *ey,
-                    const uint8_t *ep, int ksize, float *out_signed, float *out_unsigned,
-                    int32_t *out_count)
+                    const uint8_t *ep, int ksize, const double *cam, float *out_signed,
+                    float *out_unsigned, int32_t *out_count)
 {
     int32_t *cnt = (int32_t *)calloc((size_t)W * H, sizeof(int32_t));
     for (int64_t i = 0; i < n; ++i) {
@@ -705,6 +739,14 @@ void or_event_frame(int W, int H, int64_t n, const uint16_t *ex, const uint16_t 
         cnt[(size_t)ey[i] * W + ex[i]] += ep[i] ? 1 : -1;
     }
     if (out_count) memcpy(out_count, cnt, sizeof(int32_t) * (size_t)W * H);
+    float *img = (float *)malloc(sizeof(float) * (size_t)W * H);
+    for (size_t i = 0; i < (size_t)W * H; ++i) img[i] = (float)cnt[i];
+    if (cam) {
+        float *und = (float *)malloc(sizeof(float) * (size_t)W * H);
+        or_undistort(img, W, H, cam, und);
+        free(img);
+        img = und;
+    }
     double sigma = 0.3 * ((ksize - 1) * 0.5 - 1.0) + 0.8;
     double kw[64], ksum = 0;
     int r = ksize / 2;
@@ -722,7 +764,7 @@ void or_event_frame(int W, int H, int64_t n, const uint16_t *ex, const uint16_t 
             for (int k = -r; k <= r; ++k) {
                 int xx = x + k;
                 xx = xx < 0 ? 0 : (xx >= W ? W - 1 : xx);
-                s += kw[k + r] * (double)cnt[(size_t)y * W + xx];
+                s += kw[k + r] * (double)img[(size_t)y * W + xx];
             }
             tmp[(size_t)y * W + x] = s;
         }
@@ -746,6 +788,7 @@ void or_event_frame(int W, int H, int64_t n, const uint16_t *ex, const uint16_t 
         if (out_unsigned) out_unsigned[i] = fabsf(v);
     }
     free(cnt);
+    free(img);
     free(tmp);
     free(blur);
 }

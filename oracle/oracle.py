@@ -70,8 +70,9 @@ def lib():
                                              _opt(f64p), _opt(f64p)]
         L.or_loss.restype = C.c_double
         L.or_loss.argtypes = [C.c_int64, f32p, f32p, f32p, C.c_int, _opt(f64p), _opt(f64p)]
-        L.or_event_frame.argtypes = [C.c_int, C.c_int, C.c_int64, u16p, u16p, u8p, C.c_int, f32p,
-                                     _opt(f32p), _opt(i32p)]
+        L.or_event_frame.argtypes = [C.c_int, C.c_int, C.c_int64, u16p, u16p, u8p, C.c_int, _opt(f64p),
+                                     f32p, _opt(f32p), _opt(i32p)]
+        L.or_undistort.argtypes = [f32p, C.c_int, C.c_int, f64p, f32p]
         L.or_resize_nearest.argtypes = [f32p, C.c_int, C.c_int, f32p, C.c_int, C.c_int]
         _lib = L
     return _lib
@@ -250,7 +251,8 @@ def loss_f64(I_last, I_next, E, unsigned=False):
     return float(np.sqrt(np.sum(r * r)))
 
 
-def event_frame(W, H, x, y, p, ksize=9):
+def event_frame(W, H, x, y, p, ksize=9, camera=None):
+    """camera: None (no undistortion) or (fx, fy, cx, cy, k1, k2, p1, p2, k3)."""
     x, y, p = _c(x, np.uint16), _c(y, np.uint16), _c(p, np.uint8)
     s = np.zeros((H, W), np.float32)
     u = np.zeros((H, W), np.float32)
@@ -258,8 +260,17 @@ def event_frame(W, H, x, y, p, ksize=9):
     n = x.shape[0]
     if n == 0:
         x = np.zeros(1, np.uint16); y = np.zeros(1, np.uint16); p = np.zeros(1, np.uint8)
-    lib().or_event_frame(W, H, n, x, y, p, ksize, s, u, c)
+    cam = None if camera is None else np.ascontiguousarray(camera, np.float64)
+    lib().or_event_frame(W, H, n, x, y, p, ksize, cam, s, u, c)
     return s, u, c
+
+
+def undistort(img, camera):
+    img = _c(img, np.float32)
+    H, W = img.shape
+    out = np.zeros((H, W), np.float32)
+    lib().or_undistort(img, W, H, np.ascontiguousarray(camera, np.float64), out)
+    return out
 
 
 def resize_nearest(img, dw, dh):

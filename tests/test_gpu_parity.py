@@ -330,6 +330,12 @@ def test_event_frame_gpu_vs_oracle():
         np.testing.assert_array_equal(sig[l][0].cpu().numpy(), lv[l])
     z, _ = event_frames(_t(x[:0]), _t(y[:0]), _t(p[:0]), W, H, 9, 1, DEV)
     assert not z[0].any()
+    # with the desk_normal1 intrinsics and distortion (configs/VECTOR/desk_normal1_config.yaml)
+    cam = (327.32749, 327.46184, 304.97749, 235.37621, -0.031982, 0.041966, -0.000507, -0.001031, 0.0)
+    sig_d, _ = event_frames(_t(x), _t(y), _t(p), W, H, 9, 1, DEV, camera=cam)
+    sd_ref, _, _ = oracle.event_frame(W, H, x, y, p, 9, camera=cam)
+    np.testing.assert_allclose(sig_d[0][0].cpu().numpy(), sd_ref, atol=1e-6 * np.abs(sd_ref).max())
+    assert np.abs(sd_ref - s_ref).max() > 1e-3 * np.abs(s_ref).max()
 
 
 # ------------------------------------------------------- batched vs plain --

@@ -1,0 +1,82 @@
+"""CPU tests of map / event / trajectory I/O (gsevt.io)."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from gsevt import io as gio
+from gsevt import pose as gpose
+
+
+def test_ply_round_trip_and_layout(tmp_path):
+    rng = np.random.default_rng(0)
+    n = 50
+    xyz = rng.normal(size=(n, 3)).astype(np.float32)
+    feats = rng.normal(size=(n, 16, 3)).astype(np.float32)
+    op = rng.normal(size=(n, 1)).astype(np.float32)
+    sc = rng.normal(-4, 0.5, size=(n, 3)).astype(np.float32)
+    rot = rng.normal(size=(n, 4)).astype(np.float32)
+    p = str(tmp_path / "map.ply")
+    gio.save_ply(p, xyz, feats, op, sc, rot)
+    raw = gio.load_ply(p)
+    for k, v in (("xyz", xyz), ("features", feats), ("opacity", op), ("scaling", sc), ("rotation", rot)):
+        assert np.array_equal(raw[k], v), k
+    # channel-major f_rest layout: f_rest_{c * 15 + k} is coefficient k + 1 of channel c
+    hdr = open(p, "rb").read().split(b"end_header\n")[0].decode()
+    assert "property float f_rest_44" in hdr and "property float f_rest_45" not in hdr
+    m = gio.activate(raw)
+    np.testing.assert_allclose(np.linalg.norm(m["rot"], axis=1), 1.0, atol=1e-6)
+    np.testing.assert_allclose(m["opacity"], 1 / (1 + np.exp(-op[:, 0])), rtol=1e-6)
+    np.testing.assert_allclose(m["scale"], np.exp(sc), rtol=1e-6)
+
+
+def test_ascii_ply(tmp_path):
+    p = str(tmp_path / "a.ply")
+    names = ["x", "y", "z", "f_dc_0", "f_dc_1", "f_dc_2", "opacity", "scale_0", "scale_1", "scale_2",
+             "rot_0", "rot_1", "rot_2", "rot_3"]
+    with open(p, "w") as f:
+        f.write("ply\nformat ascii 1.0\nelement vertex 2\n")
+        f.write("".join("property float %s\n" % n for n in names) + "end_header\n")
+        f.write(" ".join(str(float(i)) for i in range(14)) + "\n")
+        f.write(" ".join(str(float(i + 1)) for i in range(14)) + "\n")
+    raw = gio.load_ply(p, sh_degree=0)
+    assert raw["xyz"].tolist() == [[0, 1, 2], [1, 2, 3]]
+    assert raw["features"].shape == (2, 1, 3) and raw["rotation"][1].tolist() == [11, 12, 13, 14]
+
+
+def test_events_txt_windows(tmp_path):
+    rng = np.random.default_rng(1)
+    n = 1050
+    ts = np.sort(rng.integers(0, 10 ** 6, n))
+    x, y, pol = rng.integers(0, 640, n), rng.integers(0, 480, n), rng.integers(0, 2, n)
+    p = str(tmp_path / "events.txt")
+    with open(p, "w") as f:
+        for i in range(n):
+            f.write("%d %d %d %d\n" % (ts[i], x[i], y[i], pol[i]))
+    wins = gio.load_events_txt(p, 100)
+    assert len(wins) == 10  # leftover 50 events dropped
+    assert np.array_equal(wins[3].x, x[300:400]) and np.array_equal(wins[3].y, y[300:400])
+    assert np.array_equal(wins[3].polarity, pol[300:400]) and wins[3].size() == 100
+    assert abs(wins[0].duration() - (ts[99] - ts[0]) / 1e6) < 1e-12
+    assert len(gio.load_events_txt(p, 100, array_nums=4)) == 4
+    late = gio.load_events_txt(p, 100, start_time=int(ts[500]))
+    assert late[0].ts[0] >= ts[500]
+
+
+def test_tum_writer(tmp_path):
+    R = gpose.exp_so3([0.3, -0.2, 0.5])
+    t = np.array([1.0, 2.0, 3.0])
+    p = str(tmp_path / "traj.txt")
+    gio.write_tum(p, [(0.5, R, t)])
+    f = [float(v) for v in open(p).read().split()]
+    assert f[:4] == [0.5, 1.0, 2.0, 3.0]
+    qx, qy, qz, qw = f[4:]
+    # rebuild R from the quaternion
+    Rq = np.array([[1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qz * qw), 2 * (qx * qz + qy * qw)],
+                   [2 * (qx * qy + qz * qw), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qx * qw)],
+                   [2 * (qx * qz - qy * qw), 2 * (qy * qz + qx * qw), 1 - 2 * (qx * qx + qy * qy)]])
+    np.testing.assert_allclose(Rq, R, atol=1e-12)
+    for Rm in (gpose.exp_so3([math.pi - 1e-3, 0.1, 0.0]), gpose.exp_so3([0.0, math.pi * 0.999, 0.0])):
+        q = gio.rotation_to_quaternion_xyzw(Rm)
+        assert abs(np.linalg.norm(q) - 1) < 1e-12

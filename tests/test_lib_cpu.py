@@ -54,8 +54,8 @@ def test_argument_validation_without_gpu():
     f = _lib.Frame()
     f.L.num_views = 0
     assert L.gsevt_bin_and_sort(C.byref(f), 0, None) == -1
-    assert L.gsevt_events_accumulate(10, None, None, None, 64, 48, 9, 3, None, None, None, None) == -1
-    assert L.gsevt_events_accumulate(0, None, None, None, 64, 48, 8, 1, C.c_void_p(16), C.c_void_p(16), None,
-                                     None) == -1  # even kernel size
+    assert L.gsevt_events_accumulate(10, None, None, None, 64, 48, None, 9, 3, None, None, None, None) == -1
+    assert L.gsevt_events_accumulate(0, None, None, None, 64, 48, None, 8, 1, C.c_void_p(16), C.c_void_p(16),
+                                     None, None) == -1  # even kernel size
     assert L.gsevt_pack_map(10, None, None, None, None, None, None, 16, 1.0, None, None) == -1
     assert L.gsevt_chain_view_grad(None, None, 0.0, None, None, None, None) == -1

@@ -328,3 +328,36 @@ def test_synthetic_events_counts():
     x, y, p, ts = synthetic.synth_events(a, b, 3000, 1)
     assert x.shape[0] == 3000 and ts.shape[0] == 3000 and np.all(np.diff(ts) >= 0)
     assert x.max() < 32 and y.max() < 24
+
+
+def test_undistort_oracle():
+    """Zero distortion is the identity; otherwise the result equals an independent numpy
+    evaluation of the same OpenCV model (FP64 map, 1/32-pixel rounding, bilinear, zero
+    border)."""
+    rng = np.random.default_rng(4)
+    W, H = 64, 48
+    img = rng.normal(size=(H, W)).astype(np.float32)
+    cam0 = (60.0, 61.0, 31.5, 23.2, 0.0, 0.0, 0.0, 0.0, 0.0)
+    assert np.array_equal(oracle.undistort(img, cam0), img)
+    cam = (60.0, 61.0, 31.5, 23.2, -0.031982, 0.041966, -0.000507, -0.001031, 0.0)  # desk_normal1 factors
+    got = oracle.undistort(img, cam)
+    fx, fy, cx, cy, k1, k2, p1, p2, k3 = cam
+    v, u = np.mgrid[0:H, 0:W].astype(np.float64)
+    x, y = (u - cx) / fx, (v - cy) / fy
+    r2 = x * x + y * y
+    kr = 1 + ((k3 * r2 + k2) * r2 + k1) * r2
+    xd = x * kr + p1 * 2 * x * y + p2 * (r2 + 2 * x * x)
+    yd = y * kr + p1 * (r2 + 2 * y * y) + p2 * 2 * x * y
+    iu = np.rint((fx * xd + cx) * 32).astype(np.int64)
+    iv = np.rint((fy * yd + cy) * 32).astype(np.int64)
+    ix, iy = iu >> 5, iv >> 5
+    ax, ay = (iu & 31) / 32.0, (iv & 31) / 32.0
+    ref = np.zeros((H, W))
+    for dy in (0, 1):
+        for dx in (0, 1):
+            sx, sy = ix + dx, iy + dy
+            ok = (sx >= 0) & (sy >= 0) & (sx < W) & (sy < H)
+            w = (ax if dx else 1 - ax) * (ay if dy else 1 - ay)
+            ref[ok] += w[ok] * img[sy[ok], sx[ok]]
+    np.testing.assert_allclose(got, ref, atol=1e-5)
+    assert not np.array_equal(got, img)
