@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
             const float Io = p.image[p.views[other].pix_offset + lp];
             const float Is = p.image[pix];
             const float dI = V.pair_role == 0 ? (Io - Is) : (Is - Io);
-            const float e = pr.event[lp];
+            const float e = (pr.unsigned_mode && pr.event_abs) ? pr.event_abs[lp] : pr.event[lp];
             const float n = (float)((double)dI / s);
             const float ng = (float)((1.0 - cross / s) / L);
             float g;

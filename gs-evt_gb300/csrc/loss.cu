@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
         int i = base + k * GS_BLOCK + threadIdx.x;
         if (i < P) {
             float d = image[Vn.pix_offset + i] - image[Vl.pix_offset + i];
-            float e = __ldg(pr.event + i);
+            float e = (pr.unsigned_mode && pr.event_abs) ? __ldg(pr.event_abs + i) : __ldg(pr.event + i);
             s2 = fmaf(d, d, s2);
             e2 = fmaf(e, e, e2);
             cr = pr.unsigned_mode ? fmaf(fabsf(d), fabsf(e), cr) : fmaf(d, e, cr);

@@ -176,11 +176,12 @@ __device__ inline void write_view_pose(gsevt_view *V, const double *R, const dou
 }
 
 __global__ void k_track_finalize(gsevt_view *views, gsevt_pose_state *poses, int num_poses, Workspace ws,
-                                 const double *loss, const gsevt_pair *pairs, int num_pairs)
+                                 const double *loss, gsevt_pair *pairs, int num_pairs)
 {
     int pi = blockIdx.x * blockDim.x + threadIdx.x;
     if (pi >= num_poses) return;
     gsevt_pose_state &S = poses[pi];
+    if (S.control && S.frozen) return;  // this problem's level is finished
     const float h = (float)(S.delta_tau * 0.5);
     float gpose[6] = {0, 0, 0, 0, 0, 0}, gvel[6] = {0, 0, 0, 0, 0, 0};
     const int vids[2] = {S.last_view, S.next_view};
@@ -212,6 +213,21 @@ __global__ void k_track_finalize(gsevt_view *views, gsevt_pose_state *poses, int
     if (!finite) {
         atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
         return;
+    }
+    // stage control: the velocity learning-rate ramp of the fine stage
+    // (utils/tracker.py:188-202): k = optim_iter - start_vel_opt_iter,
+    // fraction = k / (max_optim_iter / 2) for 1 <= k <= max_optim_iter / 2, else 1;
+    // theta, rho use lr * fraction and w, v use lr * (1 - fraction).
+    if (S.control) {
+        if (S.opt_vel) {
+            const double fnum = 0.5 * (double)S.max_iter;
+            const int k = S.level_iter - S.start_vel;
+            const double frac = (k >= 1 && (double)k <= fnum) ? (double)k / fnum : 1.0;
+            S.lr_scale[0] = S.lr_scale[1] = frac;
+            S.lr_scale[2] = S.lr_scale[3] = 1.0 - frac;
+        } else {
+            S.lr_scale[0] = S.lr_scale[1] = S.lr_scale[2] = S.lr_scale[3] = 1.0;
+        }
     }
     // Adam with torch's update rule; the parameter is 0 before every step (the deltas are
     // reset after each update), so the new delta is the step itself
@@ -253,6 +269,35 @@ __global__ void k_track_finalize(gsevt_view *views, gsevt_pose_state *poses, int
     for (int i = 0; i < 9; ++i) S.R[i] = Rn[i];
     for (int i = 0; i < 3; ++i) S.t[i] = tn[i];
     S.iter += 1;
+    if (S.control) {
+        // losses.append(loss); converged = mean |diff(last 11 losses)| < threshold
+        // (utils/tracker.py:65-76, 213-217); stage switch / level end (:224-240)
+        S.hist[S.hist_n % 11] = S.loss;
+        S.hist_n += 1;
+        bool converged = false;
+        if (S.hist_n > 10) {
+            double acc = 0.0;
+            for (int q = 0; q < 10; ++q) {
+                const double a = S.hist[(S.hist_n - 11 + q) % 11], b = S.hist[(S.hist_n - 10 + q) % 11];
+                acc += fabs(b - a);
+            }
+            converged = acc / 10.0 < S.conv_thr;
+        }
+        if (converged) {
+            if (!S.opt_vel) {
+                S.opt_vel = 1;
+                S.start_vel = S.level_iter;
+                for (int p = 0; p < num_pairs; ++p)
+                    if (pairs[p].pose == pi) pairs[p].unsigned_mode = 0;
+            } else {
+                S.frozen = 1;
+            }
+        }
+        if (!S.frozen) {
+            if (!S.opt_vel ? (S.level_iter >= S.max_iter) : (S.level_iter >= S.start_vel + S.max_iter)) S.frozen = 1;
+        }
+        S.level_iter += 1;
+    }
     // rewrite the pair's view entries for the next iteration
     for (int k = 0; k < 2; ++k) {
         double Rs[9], ts[3];
@@ -337,7 +382,7 @@ int gs_launch_track_finalize(const gsevt_frame *f, const Workspace &ws, gsevt_po
                              const double *loss, cudaStream_t s)
 {
     k_track_finalize<<<(num_poses + 63) / 64, 64, 0, s>>>((gsevt_view *)f->views, poses, num_poses, ws, loss,
-                                                          f->pairs, f->L.num_pairs);
+                                                          (gsevt_pair *)f->pairs, f->L.num_pairs);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

@@ -59,8 +59,8 @@ class MapGrads(C.Structure):
 
 class Pair(C.Structure):
     _fields_ = [("last_view", C.c_int32), ("next_view", C.c_int32), ("event", C.c_void_p),
-                ("unsigned_mode", C.c_int32), ("pose", C.c_int32), ("block_offset", C.c_int32),
-                ("num_blocks", C.c_int32)]
+                ("event_abs", C.c_void_p), ("unsigned_mode", C.c_int32), ("pose", C.c_int32),
+                ("block_offset", C.c_int32), ("num_blocks", C.c_int32)]
 
 
 class Layout(C.Structure):
@@ -85,7 +85,9 @@ class PoseState(C.Structure):
                 ("step", C.c_int32 * 4), ("opt_vel", C.c_int32), ("last_view", C.c_int32),
                 ("next_view", C.c_int32), ("iter", C.c_int32), ("pad", C.c_int32),
                 ("fx", C.c_float), ("fy", C.c_float), ("loss", C.c_double),
-                ("grad", C.c_double * 12)]
+                ("grad", C.c_double * 12), ("control", C.c_int32), ("frozen", C.c_int32),
+                ("level_iter", C.c_int32), ("start_vel", C.c_int32), ("hist_n", C.c_int32),
+                ("max_iter", C.c_int32), ("conv_thr", C.c_double), ("hist", C.c_double * 11)]
 
 
 _lib = None

@@ -42,7 +42,7 @@ def _field(name):
 
 
 class BatchedTracker:
-    def __init__(self, maps, problems, key_capacity=None, device="cuda"):
+    def __init__(self, maps, problems, key_capacity=None, device="cuda", key_margin=1.3):
         """maps: list of dicts with xyz, opacity, sh, scale, rot (numpy or tensors) or
         already-packed tensors under "packed" with "n"."""
         self.device = torch.device(device)
@@ -71,8 +71,8 @@ class BatchedTracker:
                 views.append(ViewSpec(p.width, p.height, p.map_index, R=np.eye(3), t=np.zeros(3), P=P,
                                       campos=np.zeros(3), tanfovx=np.tan(fovx / 2), tanfovy=np.tan(fovy / 2),
                                       pair=i, pair_role=role))
-            ev = p.event_unsigned if (p.unsigned and p.event_unsigned is not None) else p.event_signed
-            pairs.append({"last": 2 * i, "next": 2 * i + 1, "event": ev, "unsigned": p.unsigned, "pose": i})
+            pairs.append({"last": 2 * i, "next": 2 * i + 1, "event": p.event_signed, "event_abs": p.event_unsigned,
+                          "unsigned": p.unsigned, "pose": i})
         self.frame = GSFrame(specs, views, channels=1, pairs=pairs, key_capacity=key_capacity or (1 << 20),
                              device=self.device)
         self.num = len(self.problems)
@@ -80,7 +80,7 @@ class BatchedTracker:
         self._init_states()
         self.graph = None
         if key_capacity is None:
-            self.fit_capacity()
+            self.fit_capacity(key_margin)
 
     # ---------------------------------------------------------------- state --
     def _init_states(self):
@@ -127,6 +127,10 @@ class BatchedTracker:
                     loss=g("loss", 1)[:, 0], grad=g("grad", 12),
                     iter=i32[:, _field("iter") // 4])
 
+    def states_raw(self):
+        i32 = self.state.view(torch.int32).view(self.num, self._sz // 4).cpu().numpy()
+        return {"frozen": i32[:, _field("frozen") // 4], "level_iter": i32[:, _field("level_iter") // 4]}
+
     # ----------------------------------------------------------------- run --
     def fit_capacity(self, margin=1.3):
         f = self.frame
@@ -164,3 +168,180 @@ class BatchedTracker:
     def check_status(self):
         st, k = self.frame.status()
         return st, k
+
+
+class BatchedSequenceTracker:
+    """The reference's per-frame tracking loop (utils/tracker.py:105-287) for many problems at
+    once: per frame, constant-velocity prediction (camera.py:183-201), the event pyramid,
+    then per pyramid level 2 -> 0 the coarse / fine Adam stages with slope convergence, run
+    on the device for all problems in lockstep (finished problems are frozen), and after
+    five frames the weighted velocity update (camera.py:157-181).
+
+    cameras: list of (map_index, width, height, fx, fy) per problem.  One frame per pyramid
+    level shares the maps and one device pose-state array; each level's iteration is a
+    CUDA graph captured once and replayed for every frame."""
+
+    def __init__(self, maps, cameras, lr=DEFAULT_LR, max_optim_iter=200, converged_threshold=1e-4, levels=3,
+                 poll_every=10, device="cuda"):
+        from .pose import exp_se3
+        self.device = torch.device(device)
+        self.levels, self.max_iter, self.thr, self.poll = levels, int(max_optim_iter), float(converged_threshold), poll_every
+        self.cameras = cameras
+        self.packed = []
+        for m in maps:
+            if "packed" in m:
+                self.packed.append({"packed": m["packed"], "n": int(m["n"])})
+            else:
+                t = lambda a: torch.as_tensor(np.asarray(a) if not torch.is_tensor(a) else a,
+                                              dtype=torch.float32).to(self.device).contiguous()
+                n = int(np.asarray(m["xyz"]).shape[0])
+                pk = pack_map(t(m["xyz"]), t(m["opacity"]), t(m["sh"]), scales=t(m["scale"]), rotations=t(m["rot"]))
+                self.packed.append({"packed": pk, "n": n})
+        self.lr = lr
+        self.trackers, self.ev = [], []
+        for l in range(levels):
+            sc = 0.5 ** l
+            bufs, probs = [], []
+            for (mi, W, H, fx, fy) in cameras:
+                w, h = int(W * sc), int(H * sc)
+                es = torch.zeros(w * h, dtype=torch.float32, device=self.device)
+                eu = torch.zeros(w * h, dtype=torch.float32, device=self.device)
+                bufs.append((es, eu))
+                probs.append(Problem(mi, np.eye(3), np.zeros(3), np.zeros(3), np.zeros(3), 0.01, w, h, fx * sc,
+                                     fy * sc, es, eu, lr=lr))
+            self.ev.append(bufs)
+            # capacity is fitted on the first frame
+            self.trackers.append(BatchedTracker(self.packed, probs, key_capacity=1 << 20, device=self.device))
+        self.order = self.trackers[0].order
+        # event buffers in the trackers' (map-grouped) problem order
+        self.ev = [[bufs[pi] for pi in self.order] for bufs in self.ev]
+        self.num = len(cameras)
+        self.state = self.trackers[0].state
+        for tr in self.trackers[1:]:
+            tr.state = self.state
+        self.fitted = False
+        self.iterations = 0
+
+    def _set_unsigned(self, tr, flags):
+        sz = C.sizeof(_lib.Pair)
+        off = _lib.Pair.unsigned_mode.offset // 4
+        tab = tr.frame.pair_table.view(torch.int32).view(tr.num, sz // 4)
+        tab[:, off].copy_(torch.as_tensor(flags, dtype=torch.int32))
+
+    def _host_states(self):
+        return self.state.view(torch.uint8).cpu().numpy().copy()
+
+    def track(self, init_states, windows):
+        """init_states: per problem (R, t, lin_vel, ang_vel) (world -> camera, FP64);
+        windows: per frame, a list with one EventArray per problem (or a tuple
+        (x, y, polarity, ts, camera_or_None)).  Returns per problem a list of
+        (timestamp, R, t)."""
+        from .events import event_frames
+        from .pose import exp_se3, matrix, so3_log
+        n = self.num
+        arr = (_lib.PoseState * n)()
+        # problems are stored in map order (self.order)
+        for slot, pi in enumerate(self.order):
+            R, t, lv, av = init_states[pi]
+            s = arr[slot]
+            for k in range(9):
+                s.R[k] = float(np.asarray(R).reshape(9)[k])
+            for k in range(3):
+                s.t[k], s.lin_vel[k], s.ang_vel[k] = float(t[k]), float(lv[k]), float(av[k])
+            for k in range(4):
+                s.lr[k], s.lr_scale[k] = float(self.lr[k]), 1.0
+            s.last_view, s.next_view = 2 * slot, 2 * slot + 1
+            s.control, s.max_iter, s.conv_thr = 1, self.max_iter, self.thr
+        host = arr
+        traj = [[] for _ in range(n)]
+        last_dtau = [0.0] * n
+        for fi, frame in enumerate(windows):
+            init_pose = []
+            for slot, pi in enumerate(self.order):
+                w = frame[pi]
+                ts = w.ts if hasattr(w, "ts") else w[3]
+                dtau = float(ts[-1] - ts[0]) / 1e6 if len(ts) else 0.0
+                s = host[slot]
+                tau = (dtau + last_dtau[slot]) / 2
+                u = np.concatenate([np.asarray(s.lin_vel[:]) * tau, np.asarray(s.ang_vel[:]) * tau])
+                T = exp_se3(u) @ matrix(np.asarray(s.R[:]).reshape(3, 3), np.asarray(s.t[:]))
+                # the frame's initial status is the predicted pose (tracker.py:133-139)
+                init_pose.append((T[:3, :3].copy(), T[:3, 3].copy()))
+                for k in range(9):
+                    s.R[k] = float(T[:3, :3].reshape(9)[k])
+                for k in range(3):
+                    s.t[k] = float(T[k, 3])
+                s.delta_tau = dtau
+                for k in range(12):
+                    s.m[k] = s.v[k] = 0.0
+                for k in range(4):
+                    s.step[k] = 0
+                # event pyramid of this problem into every level's buffers
+                x, y, pol = (w.x, w.y, w.polarity) if hasattr(w, "x") else w[:3]
+                cam = None if hasattr(w, "x") else w[4]
+                mi, W, H, fx, fy = self.cameras[pi]
+                tt = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
+                sig, uns = event_frames(tt(x), tt(y), tt(pol), W, H, 9, self.levels, self.device, camera=cam)
+                for l in range(self.levels):
+                    self.ev[l][slot][0].copy_(sig[l].reshape(-1))
+                    self.ev[l][slot][1].copy_(uns[l].reshape(-1))
+            for lvl in range(self.levels - 1, -1, -1):
+                tr = self.trackers[lvl]
+                opt_vel = int(lvl != self.levels - 1)
+                for slot in range(n):
+                    s = host[slot]
+                    s.frozen, s.level_iter, s.start_vel, s.hist_n, s.opt_vel = 0, 0, 0, 0, opt_vel
+                    for k in range(4):
+                        s.lr_scale[k] = 1.0
+                self.state.copy_(torch.frombuffer(bytearray(bytes(host)), dtype=torch.uint8))
+                self._set_unsigned(tr, [1 - opt_vel] * n)
+                check(lib().gsevt_track_init_views(_ptr(tr.frame.view_table), _ptr(self.state), n, _stream()),
+                      "gsevt_track_init_views")
+                if not self.fitted:
+                    tr.fit_capacity(margin=2.0)
+                if tr.graph is None:
+                    tr.graph = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(tr.graph):
+                        tr.step()
+                    # capture does not run the work: restore the level's starting state
+                    self.state.copy_(torch.frombuffer(bytearray(bytes(host)), dtype=torch.uint8))
+                    self._set_unsigned(tr, [1 - opt_vel] * n)
+                    check(lib().gsevt_track_init_views(_ptr(tr.frame.view_table), _ptr(self.state), n, _stream()),
+                          "gsevt_track_init_views")
+                limit = 2 * self.max_iter + 2
+                done_iters = 0
+                while done_iters < limit:
+                    for _ in range(self.poll):
+                        tr.graph.replay()
+                    done_iters += self.poll
+                    st = tr.states_raw()
+                    if all(int(x) for x in st["frozen"]):
+                        break
+                self.iterations += done_iters
+                st_b = self._host_states()
+                host = (_lib.PoseState * n).from_buffer_copy(st_b.tobytes())
+                stat, _ = tr.frame.status()
+                if stat & _lib.STATUS_KEY_OVERFLOW:
+                    raise RuntimeError("key capacity overflow at pyramid level %d" % lvl)
+            self.fitted = True
+            for slot, pi in enumerate(self.order):
+                s = host[slot]
+                w = frame[pi]
+                ts = w.ts if hasattr(w, "ts") else w[3]
+                dtau = float(ts[-1] - ts[0]) / 1e6 if len(ts) else 0.0
+                if fi >= 5:
+                    R0, t0 = init_pose[slot]
+                    R1 = np.asarray(s.R[:]).reshape(3, 3)
+                    t1 = np.asarray(s.t[:])
+                    D = matrix(R1, t1) @ np.linalg.inv(matrix(R0, t0))
+                    tau = (dtau + last_dtau[slot]) / 2
+                    lv = D[:3, 3] / tau
+                    av = so3_log(D[:3, :3]) / tau
+                    for k in range(3):
+                        s.lin_vel[k] = 0.5 * lv[k] + 0.5 * s.lin_vel[k]
+                        s.ang_vel[k] = 0.5 * av[k] + 0.5 * s.ang_vel[k]
+                last_dtau[slot] = dtau
+                stamp = (ts[0] + (ts[-1] - ts[0]) / 2) / 1e6 if len(ts) else 0.0
+                traj[pi].append((stamp, np.asarray(s.R[:]).reshape(3, 3).copy(), np.asarray(s.t[:]).copy()))
+        self.state.copy_(torch.frombuffer(bytearray(bytes(host)), dtype=torch.uint8))
+        return traj

@@ -178,6 +178,8 @@ class GSFrame:
                 s = _lib.Pair()
                 s.last_view, s.next_view = p["last"], p["next"]
                 s.event = p["event"].data_ptr()
+                ea = p.get("event_abs")
+                s.event_abs = None if ea is None else ea.data_ptr()
                 s.unsigned_mode = int(p.get("unsigned", False))
                 s.pose = int(p.get("pose", 0))
                 s.block_offset, s.num_blocks = lb_, nb

@@ -113,7 +113,8 @@ typedef struct gsevt_map_grads {
  * utils/tracker.py:93-103). */
 typedef struct gsevt_pair {
     int32_t last_view, next_view;
-    const float *event;      /* [H][W] event frame: signed, or |E| when unsigned_mode */
+    const float *event;      /* [H][W] signed event frame E */
+    const float *event_abs;  /* [H][W] |E| (unsigned mode); NULL: use |event| */
     int32_t unsigned_mode;   /* 0: L = ||n - E||, 1: L = || |n| - |E| || */
     int32_t pose;            /* pose state this pair belongs to (batched tracker) */
     int32_t block_offset;    /* first loss-reduction block of this pair */
@@ -261,6 +262,18 @@ typedef struct gsevt_pose_state {
     float fx, fy;                /* focal lengths of the rendered views */
     double loss;                 /* last loss */
     double grad[12];             /* last gradient (theta, rho, w, v) */
+    /* per-level stage control (utils/tracker.py:149-240), used when control != 0:
+     * coarse stage (opt_vel 0, unsigned loss) until the loss slope converges, then fine
+     * stage (opt_vel 1, signed loss, velocity learning-rate ramp) until it converges
+     * again or max_iter more iterations pass; then the problem is frozen. */
+    int32_t control;
+    int32_t frozen;
+    int32_t level_iter;          /* optim_iter of the current level */
+    int32_t start_vel;           /* start_vel_opt_iter */
+    int32_t hist_n;              /* losses recorded in this level */
+    int32_t max_iter;            /* max_optim_iter */
+    double conv_thr;             /* converged_threshold */
+    double hist[11];             /* last 11 losses of this level (ring) */
 } gsevt_pose_state;
 
 /* poses: device array.  Pair p's loss goes to loss_out[p] (device, nullable). */

@@ -136,3 +136,65 @@ def test_event_pyramid_levels_in_tracker_frame():
     assert torch.equal(ef.sign_pyramid[1][0], ef.sign_delta_Ie[0, ::2, ::2])
     assert torch.equal(ef.unsign_delta_Ie, ef.sign_delta_Ie.abs())
     assert abs(float(ef.sign_delta_Ie.double().norm()) - 1.0) < 1e-5
+
+
+def _sequence(sc, pk, n, frames, n_events, seed):
+    """Event windows along the scenario's constant-velocity ground truth."""
+    from gsevt.pose import exp_se3, matrix
+    cam = sc.camera
+    u = np.concatenate([sc.gt_lin, sc.gt_ang])
+    wins = []
+    for k in range(frames):
+        Tk = exp_se3(u * sc.delta_tau * k) @ matrix(sc.gt_R, sc.gt_t)
+        Tl, Tn = gpose.pair_poses(Tk[:3, :3], Tk[:3, 3], sc.gt_lin, sc.gt_ang, sc.delta_tau)
+        views = [ViewSpec(cam.width, cam.height, 0, R=T[:3, :3], t=T[:3, 3], P=cam.proj,
+                          campos=gpose.campos(T[:3, :3], T[:3, 3]), tanfovx=cam.tanfovx, tanfovy=cam.tanfovy)
+                 for T in (Tl, Tn)]
+        fr = GSFrame([MapSpec(n, packed=pk)], views, channels=1, device=DEV)
+        fr.render(exact_keys=True)
+        a, b = fr.pixels(0)[0].cpu().numpy(), fr.pixels(1)[0].cpu().numpy()
+        ex, ey, ep, ts = synthetic.synth_events(a, b, n_events, seed + k, delta_tau=sc.delta_tau)
+        wins.append(EventArray(ex, ey, ep, ts + int(k * sc.delta_tau * 1e6)))
+    return wins
+
+
+def test_batched_sequence_tracker_matches_plain_tracker():
+    """Per-frame loop (constant-velocity prediction, 3 pyramid levels, coarse/fine stages
+    with slope convergence) on the device for three problems over two maps, against the
+    plain Tracker run per problem.  Convergence decisions depend on FP32 loss values, so
+    iteration counts may differ by one; poses are compared at 5 mm / 0.3 degrees."""
+    from gsevt.batched import BatchedSequenceTracker
+    frames = 2
+    s0, pk0, _, _, _ = _scenario(20000, 320, 240, 300.0, 7, 30000)
+    s1, pk1, _, _, _ = _scenario(15000, 256, 192, 220.0, 8, 30000)
+    w0 = _sequence(s0, pk0, 20000, frames, 30000, 100)
+    w1 = _sequence(s1, pk1, 15000, frames, 30000, 200)
+    rng = np.random.default_rng(9)
+    R2, t2 = synthetic.perturb(s0.gt_R, s0.gt_t, rng, 0.03, 2.0)
+    inits = [(s0.init_R, s0.init_t, s0.init_lin, s0.init_ang), (s1.init_R, s1.init_t, s1.init_lin, s1.init_ang),
+             (R2, t2, s0.init_lin, s0.init_ang)]
+    cams = [(0, 320, 240, 300.0, 300.0), (1, 256, 192, 220.0, 220.0), (0, 320, 240, 300.0, 300.0)]
+    wins = [[w0[k], w1[k], w0[k]] for k in range(frames)]
+    bst = BatchedSequenceTracker([{"packed": pk0, "n": 20000}, {"packed": pk1, "n": 15000}], cams,
+                                 max_optim_iter=20, device=DEV)
+    traj = bst.track(inits, wins)
+    assert bst.iterations > 0
+    for pi, (sc, win) in enumerate(((s0, w0), (s1, w1), (s0, w0))):
+        cam = sc.camera
+        R0, t0, lv, av = inits[pi]
+        cfg = {"Event": {"img_width": cam.width, "img_height": cam.height, "gaussian_kernel_size": 9,
+                         "intrinsic": {"data": [cam.fx, 0, cam.width / 2, 0, cam.fy, cam.height / 2, 0, 0, 1]},
+                         "distortion_factors": [0, 0, 0, 0, 0]},
+               "Optimizer": {"cam_rot_delta": 0.004, "cam_trans_delta": 0.004, "cam_w_delta": 0.002,
+                             "cam_v_delta": 0.002, "converged_threshold": 1e-4, "max_optim_iter": 20}}
+        c = Camera(torch.tensor(R0, dtype=torch.float32), torch.tensor(t0, dtype=torch.float32),
+                   torch.tensor(av, dtype=torch.float32), torch.tensor(lv, dtype=torch.float32),
+                   cam.fovx, cam.fovy, cam.width, cam.height, device="cuda")
+        c.fx, c.fy = cam.fx, cam.fy
+        tr = Tracker(cfg, win, c, GaussianMap.from_synthetic(sc.map), None, torch.zeros(3, device=DEV), "cuda")
+        ref = tr.tracking()
+        for k in range(frames):
+            _, Rb, tb = traj[pi][k]
+            _, Rp, tp = ref[k]
+            assert np.linalg.norm(tb - tp) < 5e-3, (pi, k, tb, tp)
+            assert gpose.rotation_error_deg(Rb, Rp.astype(np.float64)) < 0.3, (pi, k)
