@@ -145,9 +145,91 @@ def make_tracker(prob, device, hypotheses=None):
         poses = [(sc.init_R, sc.init_t)]
     else:
         poses = synthetic.hypotheses(sc.gt_R, sc.gt_t, hyp, sc.seed + 5)
+    # each problem reads its own copy of the event frame
+    own = (lambda t: t.clone()) if hyp > 1 else (lambda t: t)
     probs = [Problem(0, R, t, sc.init_lin, sc.init_ang, sc.delta_tau, prob["W"], prob["H"], prob["f"], prob["f"],
-                     prob["E"], prob["E_unsigned"], opt_vel=True) for R, t in poses]
+                     own(prob["E"]), own(prob["E_unsigned"]), opt_vel=True) for R, t in poses]
     return BatchedTracker([{"packed": prob["packed"], "n": prob["n"]}], probs, device=device)
+
+
+def time_graph(bt, steps, warmup, flush):
+    import torch
+    bt.capture(warmup=max(1, warmup))
+    for _ in range(warmup):
+        bt.graph.replay()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        bt.graph.replay()
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    return sum(times) / len(times)
+
+
+def run_hypotheses(dev, flush, steps=10, warmup=3):
+    """64 pose hypotheses (0-20 cm / 0-10 degrees from ground truth) of one 500k map at
+    640x480, 128 views per launch, each hypothesis with its own event frame; iteration time
+    and the best hypothesis' error after the timed iterations."""
+    from gsevt import pose as gpose
+    prob = build_problem("hypotheses-64x2-500k", dev)
+    bt = make_tracker(prob, dev, hypotheses=64)
+    ms = time_graph(bt, steps, warmup, flush)
+    st = bt.states()
+    sc = prob["scenario"]
+    err_t = [float(np.linalg.norm(st["t"][i] - sc.gt_t)) for i in range(bt.num)]
+    err_r = [gpose.rotation_error_deg(st["R"][i], sc.gt_R) for i in range(bt.num)]
+    best = int(np.argmin(np.asarray(err_t) + np.radians(err_r)))
+    return {"workload": "hypotheses-64x2-500k", "problems": bt.num, "views": 2 * bt.num, "ms_per_iter": ms,
+            "problem_iters_per_s": 1000.0 / ms * bt.num, "keys": int(bt.num_keys),
+            "iterations_run": int(st["iter"][0]), "best_hypothesis_error_mm": 1000.0 * err_t[best],
+            "best_hypothesis_error_deg": err_r[best],
+            "l2": "flushed (256 MB write) between timed iterations"}
+
+
+def run_sequences(dev, flush, steps=10, warmup=3, count=16):
+    """16 concurrent sequences, each with its own map (log-uniform 50k-1.5M Gaussians,
+    seeds 10-25) and resolution (346x260, 640x480, 1280x720 in turn), event windows of
+    log-uniform 10k-2M events, all views in one launch per stage."""
+    import torch
+    from gsevt import synthetic
+    from gsevt import pose as gpose
+    from gsevt.batched import BatchedTracker, Problem
+    from gsevt.engine import GSFrame, MapSpec, ViewSpec, pack_map
+    from gsevt.events import event_frames
+    rng = np.random.default_rng(10)
+    res = [(346, 260), (640, 480), (1280, 720)]
+    maps, probs, total = [], [], 0
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(5e4), np.log(1.5e6))))
+        W, H = res[i % 3]
+        f = 600.0 * W / 640.0
+        ne = int(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        sc = synthetic.Scenario(n, 10 + i, W, H, f, ne)
+        m = sc.map
+        pk = pack_map(t(m["xyz"]), t(m["opacity"]), t(m["sh"]), scales=t(m["scale"]), rotations=t(m["rot"]))
+        cam = sc.camera
+        views = [ViewSpec(W, H, 0, R=T[:3, :3], t=T[:3, 3], P=cam.proj, campos=gpose.campos(T[:3, :3], T[:3, 3]),
+                          tanfovx=cam.tanfovx, tanfovy=cam.tanfovy) for T in sc.gt_pair()]
+        fr = GSFrame([MapSpec(n, packed=pk)], views, channels=1, device=dev)
+        fr.render(exact_keys=True)
+        a, b = fr.pixels(0)[0].cpu().numpy(), fr.pixels(1)[0].cpu().numpy()
+        del fr
+        ex, ey, ep, ts = synthetic.synth_events(a, b, ne, 77 + i, delta_tau=sc.delta_tau)
+        sig, uns = event_frames(t(ex), t(ey), t(ep), W, H, 9, 1, dev)
+        maps.append({"packed": pk, "n": n})
+        probs.append(Problem(i, sc.init_R, sc.init_t, sc.init_lin, sc.init_ang, sc.delta_tau, W, H, f, f,
+                             sig[0].reshape(-1).contiguous(), uns[0].reshape(-1).contiguous(), opt_vel=True))
+        total += n
+    bt = BatchedTracker(maps, probs, device=dev)
+    ms = time_graph(bt, steps, warmup, flush)
+    return {"workload": "sequences-16-uneven", "problems": count, "views": 2 * count, "gaussians_total": total,
+            "ms_per_iter": ms, "problem_iters_per_s": 1000.0 / ms * count, "keys": int(bt.num_keys),
+            "resolutions": ["%dx%d" % r for r in res], "l2": "flushed (256 MB write) between timed iterations"}
 
 
 def stage_times(bt, reps=5):
@@ -402,6 +484,8 @@ def main():
     ap.add_argument("--workload", default="adjoint-500k-640x480", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the 64-hypothesis and 16-sequence workloads reported beside the headline")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
                     help="profile: build the workload, then run warmup + steps un-graphed iterations "
                          "(for ncu launch lists; prints no timings)")
@@ -487,6 +571,10 @@ def main():
         "gpu_launches": launches_per_iter * args.steps,
         "clocks": clk,
     }
+    if not args.no_secondary:
+        del bt
+        torch.cuda.empty_cache()
+        line["secondary"] = [run_hypotheses(dev, flush), run_sequences(dev, flush)]
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(prob)
     if rank == 0:

@@ -344,4 +344,8 @@ class BatchedSequenceTracker:
                 stamp = (ts[0] + (ts[-1] - ts[0]) / 2) / 1e6 if len(ts) else 0.0
                 traj[pi].append((stamp, np.asarray(s.R[:]).reshape(3, 3).copy(), np.asarray(s.t[:]).copy()))
         self.state.copy_(torch.frombuffer(bytearray(bytes(host)), dtype=torch.uint8))
+        # Adam iterations each problem ran (a frozen problem does not count)
+        self.problem_iterations = [0] * n
+        for slot, pi in enumerate(self.order):
+            self.problem_iterations[pi] = int(host[slot].iter)
         return traj
