@@ -16,6 +16,8 @@
 //      sampled bilinearly with a zero border.
 #include "common.cuh"
 
+#include <mutex>
+
 #define EV_MAX_K 31
 
 namespace {
@@ -198,6 +200,87 @@ extern "C" int gsevt_events_accumulate(int64_t n, const uint16_t *x, const uint1
     } else {
         k_ev_to_float<<<(int)std::min<size_t>((P + 255) / 256, 152 * 8), 256, 0, s>>>(sc.count, P, sc.img);
     }
+    k_ev_blur_h<<<gh, 128, 0, s>>>(sc.img, width, height, k, sc.tmp);
+    k_ev_blur_v<<<EV_PART_BLOCKS, 256, 0, s>>>(sc.tmp, width, height, k, sc.blur, sc.part);
+    k_ev_normalize<<<1, 1024, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height, levels, out_signed,
+                                      out_unsigned);
+    GS_CUDA_CHECK();
+    return GSEVT_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// gsevt_events_accumulate_noalloc: the same launches with scratch in a fixed
+// library-owned device buffer instead of caller memory, for callers that cannot
+// allocate (see the declaration in gsevt.h).  The buffer is one per device (a
+// __device__ variable exists once per context the module is loaded into); its address
+// is looked up once per device and cached.  Concurrent calls on one device race on it.
+
+#define EV_NOALLOC_MAX_DEVICES 64
+#define EV_NOALLOC_BYTES (4 * ((((size_t)GSEVT_EVENTS_NOALLOC_MAX_PIXELS * 4) + 255) & ~(size_t)255) + \
+                          (((size_t)EV_PART_BLOCKS * 8 + 255) & ~(size_t)255))
+
+static __device__ __align__(256) unsigned char g_ev_noalloc_scratch[EV_NOALLOC_BYTES];
+static void *g_ev_noalloc_addr[EV_NOALLOC_MAX_DEVICES];
+static std::mutex g_ev_noalloc_mu;
+
+static int ev_noalloc_scratch(void **out)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GSEVT_ERR_CUDA;
+    if (dev < 0 || dev >= EV_NOALLOC_MAX_DEVICES) return GSEVT_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_ev_noalloc_mu);
+    if (!g_ev_noalloc_addr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_ev_noalloc_scratch) != cudaSuccess || !p) return GSEVT_ERR_CUDA;
+        g_ev_noalloc_addr[dev] = p;
+    }
+    *out = g_ev_noalloc_addr[dev];
+    return GSEVT_OK;
+}
+
+extern "C" int gsevt_events_accumulate_noalloc(int64_t n, const uint16_t *x, const uint16_t *y,
+                                               const uint8_t *polarity, int32_t width, int32_t height,
+                                               const double *camera, int32_t ksize, int32_t levels,
+                                               float *out_signed, float *out_unsigned, gsevt_stream_t stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (width <= 0 || height <= 0 || ksize < 1 || (ksize & 1) == 0 || ksize > EV_MAX_K || levels < 1 ||
+        !out_signed || n < 0 || (n > 0 && (!x || !y || !polarity)))
+        return GSEVT_ERR_ARG;
+    if ((int64_t)width * height > (int64_t)GSEVT_EVENTS_NOALLOC_MAX_PIXELS) return GSEVT_ERR_TOO_LARGE;
+    for (int l = 1; l < levels; ++l)
+        if ((int)(width * (1.0 / (1 << l))) < 1 || (int)(height * (1.0 / (1 << l))) < 1) return GSEVT_ERR_ARG;
+    Cam c = {};
+    if (camera) {
+        c = {camera[0], camera[1], camera[2], camera[3], camera[4], camera[5], camera[6], camera[7], camera[8]};
+        if (!(c.fx != 0.0 && c.fy != 0.0)) return GSEVT_ERR_ARG;
+    }
+    void *base = nullptr;
+    int rc = ev_noalloc_scratch(&base);
+    if (rc != GSEVT_OK) return rc;
+    EvScratch sc = ev_carve(base, width, height);
+    Kern k;
+    k.r = ksize / 2;
+    double sigma = 0.3 * ((ksize - 1) * 0.5 - 1.0) + 0.8, ws[EV_MAX_K], sum = 0.0;
+    for (int i = 0; i < ksize; ++i) {
+        double xx = i - k.r;
+        ws[i] = exp(-(xx * xx) / (2.0 * sigma * sigma));
+        sum += ws[i];
+    }
+    for (int i = 0; i < EV_MAX_K; ++i) k.w[i] = i < ksize ? (float)(ws[i] / sum) : 0.0f;
+    size_t P = (size_t)width * height;
+    // the count image accumulates with atomics and must start at zero on every call
+    if (cudaMemsetAsync(sc.count, 0, P * 4, s) != cudaSuccess) return GSEVT_ERR_CUDA;
+    if (n > 0) {
+        int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)152 * 8);
+        k_ev_count<<<blocks, 256, 0, s>>>(n, x, y, polarity, width, height, sc.count);
+        GS_CUDA_CHECK();
+    }
+    dim3 gh((width + 127) / 128, height);
+    if (camera)
+        k_ev_undistort<<<gh, 128, 0, s>>>(sc.count, width, height, c, sc.img);
+    else
+        k_ev_to_float<<<(int)std::min<size_t>((P + 255) / 256, 152 * 8), 256, 0, s>>>(sc.count, P, sc.img);
     k_ev_blur_h<<<gh, 128, 0, s>>>(sc.img, width, height, k, sc.tmp);
     k_ev_blur_v<<<EV_PART_BLOCKS, 256, 0, s>>>(sc.tmp, width, height, k, sc.blur, sc.part);
     k_ev_normalize<<<1, 1024, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height, levels, out_signed,

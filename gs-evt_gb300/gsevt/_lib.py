@@ -142,7 +142,8 @@ EXPORTED = [
     "gsevt_preprocess_fwd", "gsevt_bin_and_sort", "gsevt_blend_fwd", "gsevt_loss_fwd",
     "gsevt_blend_bwd", "gsevt_preprocess_bwd", "gsevt_chain_view_grad", "gsevt_view_from_settings",
     "gsevt_read_status", "gsevt_clear_status", "gsevt_event_scratch_bytes",
-    "gsevt_events_accumulate", "gsevt_track_step_batched", "gsevt_track_init_views",
+    "gsevt_events_accumulate", "gsevt_events_accumulate_noalloc", "gsevt_track_step_batched",
+    "gsevt_track_init_views",
 ]
 
 

@@ -242,6 +242,32 @@ int gsevt_events_accumulate(int64_t n, const uint16_t *x, const uint16_t *y,
                             const double *camera, int32_t ksize, int32_t levels, void *scratch,
                             float *out_signed, float *out_unsigned, gsevt_stream_t stream);
 
+/* gsevt_events_accumulate without the scratch argument; it allocates nothing.  This entry
+ * point has no counterpart in the reference (which builds its event frame on the host).
+ * It is for callers that cannot allocate device memory: a C sensor-driver callback that
+ * turns each event packet into a frame and holds no device allocator, a host whose device
+ * memory is all handed to its own pool, or a per-packet path that must not pay
+ * cudaMalloc's implicit device synchronisation.
+ *   - Scratch is one fixed library-owned buffer per device, sized for frames of up to
+ *     GSEVT_EVENTS_NOALLOC_MAX_PIXELS pixels (1280 x 720; 14,747,648 bytes of device
+ *     memory, taken when the library's event module loads on that device).  width *
+ *     height above that returns GSEVT_ERR_TOO_LARGE before anything is enqueued.
+ *   - Set-up: the first call on each device (with that device current) resolves the
+ *     buffer's address with cudaGetSymbolAddress and caches it; make that first call
+ *     outside any stream capture.
+ *   - The count image that must start at zero is cleared on the stream by every call;
+ *     the other scratch regions are fully overwritten.
+ *   - Calls that overlap on one device (two streams, or two host threads, without an
+ *     ordering between them) share the buffer and race: order them on one stream or
+ *     wait for the previous call to finish.
+ * Outputs and every other argument are as for gsevt_events_accumulate. */
+#define GSEVT_EVENTS_NOALLOC_MAX_PIXELS (1280 * 720)
+enum { GSEVT_ERR_TOO_LARGE = -7 };  /* frame larger than a fixed-size scratch buffer holds */
+int gsevt_events_accumulate_noalloc(int64_t n, const uint16_t *x, const uint16_t *y,
+                                    const uint8_t *polarity, int32_t width, int32_t height,
+                                    const double *camera, int32_t ksize, int32_t levels,
+                                    float *out_signed, float *out_unsigned, gsevt_stream_t stream);
+
 /* ---- batched tracker iteration (utils/tracker.py:176-240) ----
  * Per pose state (one tracking hypothesis / sequence): FP64 pose, velocity, Adam
  * moments.  One call = render all pairs, loss, adjoint, exact chain to

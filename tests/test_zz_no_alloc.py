@@ -1,0 +1,80 @@
+"""gsevt_events_accumulate_noalloc (scratch in a fixed library-owned device buffer, no
+allocation) against gsevt_events_accumulate (caller scratch), both called through the
+C ABI.  Two calls in a row on different event packets check that the second call starts
+from a cleared count image.  Kept in a file of its own that runs last, so it also runs
+after every other test has loaded and used the library."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from gsevt import _lib
+
+MAX_PIXELS = 1280 * 720
+ERR_ARG, ERR_TOO_LARGE = -1, -7
+
+
+def _bind():
+    L = C.CDLL(_lib.LIB_PATH)
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    f = L.gsevt_events_accumulate_noalloc
+    f.restype = C.c_int
+    f.argtypes = [i64, vp, vp, vp, i32, i32, C.POINTER(C.c_double), i32, i32, vp, vp, vp]
+    g = L.gsevt_events_accumulate
+    g.restype = C.c_int
+    g.argtypes = [i64, vp, vp, vp, i32, i32, C.POINTER(C.c_double), i32, i32, vp, vp, vp, vp]
+    h = L.gsevt_event_scratch_bytes
+    h.restype = C.c_size_t
+    h.argtypes = [i32, i32]
+    return f, g, h
+
+
+def test_noalloc_rejects_oversized_frames():
+    """Size and argument checks answer before anything touches a device."""
+    f, _, _ = _bind()
+    out = C.c_void_p(16)  # never written: the call returns before enqueueing work
+    assert f(0, None, None, None, 1281, 720, None, 9, 3, out, None, None) == ERR_TOO_LARGE
+    assert f(0, None, None, None, 4096, 4096, None, 9, 1, out, None, None) == ERR_TOO_LARGE
+    assert f(0, None, None, None, 640, 480, None, 8, 3, out, None, None) == ERR_ARG
+    assert f(0, None, None, None, 640, 480, None, 9, 3, None, None, None) == ERR_ARG
+
+
+def _packet(rng, n, W, H, dev):
+    x = torch.from_numpy(rng.integers(0, W, n).astype(np.uint16)).to(dev)
+    y = torch.from_numpy(rng.integers(0, H, n).astype(np.uint16)).to(dev)
+    p = torch.from_numpy(rng.integers(0, 2, n).astype(np.uint8)).to(dev)
+    return x, y, p
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("W,H,camera", [
+    (640, 480, None),
+    (346, 260, (300.0, 301.0, 170.5, 128.25, -0.12, 0.03, 1e-3, -5e-4, 0.002)),
+    (1280, 720, None),
+])
+def test_noalloc_matches_caller_scratch_entry_point(W, H, camera):
+    f, g, h = _bind()
+    dev = "cuda"
+    levels, ksize = 3, 9
+    tot = sum(int(W * 0.5 ** l) * int(H * 0.5 ** l) for l in range(levels))
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    cam = None if camera is None else (C.c_double * 9)(*camera)
+    scratch = torch.empty(int(h(W, H)), dtype=torch.uint8, device=dev)
+    rng = np.random.default_rng(W + H)
+    for call, n in enumerate((300000, 120000)):  # two calls in a row, different packets
+        x, y, p = _packet(rng, n, W, H, dev)
+        ref_s = torch.empty(tot, dtype=torch.float32, device=dev)
+        ref_u = torch.empty(tot, dtype=torch.float32, device=dev)
+        out_s = torch.full((tot,), float("nan"), dtype=torch.float32, device=dev)
+        out_u = torch.full((tot,), float("nan"), dtype=torch.float32, device=dev)
+        assert g(n, x.data_ptr(), y.data_ptr(), p.data_ptr(), W, H, cam, ksize, levels, scratch.data_ptr(),
+                 ref_s.data_ptr(), ref_u.data_ptr(), stream) == 0
+        assert f(n, x.data_ptr(), y.data_ptr(), p.data_ptr(), W, H, cam, ksize, levels,
+                 out_s.data_ptr(), out_u.data_ptr(), stream) == 0
+        torch.cuda.synchronize()
+        a, b = out_s.cpu().numpy(), ref_s.cpu().numpy()
+        assert np.isfinite(a).all() and np.abs(b).max() > 0, call
+        # same kernels and launch shapes over the same inputs: equal to FP32 rounding
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-7, err_msg="call %d" % call)
+        np.testing.assert_allclose(out_u.cpu().numpy(), np.abs(b), rtol=0, atol=1e-7, err_msg="call %d" % call)
