@@ -20,8 +20,9 @@
 // per tile in shared memory and added to the global per-slot gradients once per tile.
 //
 // Warp-level culling (both directions): each batch Gaussian gets a conservative pixel
-// box of its alpha support (gauss_box); a warp ballots which of them overlap its 16x2
-// pixel strip and walks only those, in depth order.  Gaussians outside the box cannot
+// box and quadratic form of its alpha support (gauss_box); a warp ballots which of them
+// reach its 8x4 pixel block (box overlap, then the exact ellipse-rectangle test of
+// ellipse_hits) and walks only those, in depth order.  Gaussians that fail both cannot
 // pass the per-pixel alpha test, so the decisions and results are unchanged.
 #include "common.cuh"
 
@@ -49,12 +50,12 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-struct Batch {
+template <bool RGB> struct Batch {
     float4 A[GS_BLOCK];
     float4 B[GS_BLOCK];
-    float4 C[GS_BLOCK];
+    float4 C[RGB ? GS_BLOCK : 1];
     float4 box[GS_BLOCK];  // {xmin, xmax, ymin, ymax}: outside it the Gaussian fails the alpha test
-    float thr[GS_BLOCK];   // power below this value cannot pass the alpha test
+    float4 ell[GS_BLOCK];  // {a, b, c, thr}: quadratic form of the support and power threshold
     uint32_t id[GS_BLOCK];
 };
 
@@ -62,32 +63,64 @@ struct Batch {
 // only if alpha = min(0.99, o exp(power)) >= 1/255, i.e. -power <= tau = ln(255 o).  With
 // M the conic, -power = d^T M d / 2 in exact arithmetic; the FP32 evaluation of the six
 // products and sums deviates by less than 1e-6 tr(M) |d|^2, so every pixel that can pass
-// satisfies d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the slack also covers gs_expf's
-// 2 ulp and logf).  The box of that ellipse, widened by 0.1 % + 0.5 px, therefore never
-// excludes a pixel whose per-pixel test would pass, so culling against it leaves every
-// blending decision - and the result bits - unchanged.
-// Also returns, through *thr, a power threshold: below -(ln(255 o) (1 + 1e-4) + 1e-3),
-// o exp(power) < 0.999 / 255, so alpha < 1/255 whatever exp's last bits - the exp and the
-// alpha test can be skipped there without changing any decision.
-__device__ __forceinline__ float4 gauss_box(float4 A, float4 B, float *thr)
+// satisfies Q(d) = d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the slack also covers
+// gs_expf's 2 ulp and logf).  The box of that ellipse, widened by 0.1 % + 0.5 px,
+// therefore never excludes a pixel whose per-pixel test would pass, so culling against it
+// leaves every blending decision - and the result bits - unchanged.
+// Also returns, through *ell, Q's coefficients {a, b, c} (Q = a dx^2 + 2 b dx dy + c dy^2;
+// all zero when Q is ill-conditioned, which disables the ellipse test) and a power
+// threshold thr: below -(ln(255 o) (1 + 1e-4) + 1e-3), o exp(power) < 0.999 / 255, so
+// alpha < 1/255 whatever exp's last bits - the exp and the alpha test can be skipped there
+// without changing any decision.
+__device__ __forceinline__ float4 gauss_box(float4 A, float4 B, float4 *ell)
 {
     const float o = B.w;
-    *thr = 1e30f;
+    *ell = make_float4(0.0f, 0.0f, 0.0f, 1e30f);
     if (!(o >= (1.0f / 255.0f) * 0.999f)) return make_float4(1e30f, -1e30f, 1e30f, -1e30f);
     const float tau = logf(255.0f * o) * 1.0001f + 1e-3f;
-    *thr = -tau;
+    ell->w = -tau;
     const float g = 1e-6f * (fabsf(B.x) + fabsf(B.z));
     const float a = 0.5f * B.x - g, b = 0.5f * B.y, c = 0.5f * B.z - g;
     const float det = a * c - b * b;
     if (!(a > 0.0f && c > 0.0f && det > 0.0f && tau > -1e29f && tau < 1e29f))
         return make_float4(-1e30f, 1e30f, -1e30f, 1e30f);  // no culling
+    // |b| <= 0.995 sqrt(ac): the FP32 rounding of Q stays below 1.4e-4 Q (see ellipse_hits)
+    if (b * b <= 0.99f * (a * c)) { ell->x = a; ell->y = b; ell->z = c; }
     const float hx = sqrtf(fmaxf(tau, 0.0f) * c / det) * 1.001f + 0.5f;
     const float hy = sqrtf(fmaxf(tau, 0.0f) * a / det) * 1.001f + 0.5f;
     return make_float4(A.x - hx, A.x + hx, A.y - hy, A.y + hy);
 }
 
+// Does the Gaussian's support ellipse Q(mean - p) <= tau reach the pixel rectangle
+// [x0, x1] x [y0, y1]?  Exact minimum of the convex Q over the rectangle: zero when the
+// mean is inside, else on an edge that faces the mean (at most two), where the
+// one-dimensional minimum is clamped to the edge.  Any pixel that passes the alpha test
+// has Q <= tau, so min Q <= tau; the FP32 value computed here exceeds min Q by at most
+// 1.4e-4 Q (|b| <= 0.995 sqrt(ac) bounds a dx^2 + c dy^2 by 400 Q) plus a second-order
+// term from the rounded edge minimiser, both far below the slack of the comparison
+// (tau * 1.001 + 0.01).  So this never rejects a Gaussian a pixel of the rectangle blends.
+__device__ __forceinline__ bool ellipse_hits(float mx, float my, float4 E, float x0, float x1, float y0, float y1)
+{
+    const bool inx = mx >= x0 && mx <= x1, iny = my >= y0 && my <= y1;
+    if (inx && iny) return true;
+    const float a = E.x, b = E.y, c = E.z;
+    float q = 1e30f;
+    if (!inx) {
+        const float dx = mx - (mx < x0 ? x0 : x1);
+        const float dy = fminf(fmaxf(-__fdividef(b * dx, c), my - y1), my - y0);
+        q = (a * dx) * dx + 2.0f * ((b * dx) * dy) + (c * dy) * dy;
+    }
+    if (!iny) {
+        const float dy = my - (my < y0 ? y0 : y1);
+        const float dx = fminf(fmaxf(-__fdividef(b * dy, a), mx - x1), mx - x0);
+        q = fminf(q, (a * dx) * dx + 2.0f * ((b * dx) * dy) + (c * dy) * dy);
+    }
+    return q <= -E.w * 1.001f + 0.01f;
+}
+
 // Issue the copies of batch `r` of the tile range into buffer `buf`.
-__device__ __forceinline__ void load_batch(const BlendParams &p, Batch &buf, uint2 range, int r)
+template <bool RGB>
+__device__ __forceinline__ void load_batch(const BlendParams &p, Batch<RGB> &buf, uint2 range, int r)
 {
     uint32_t idx = range.x + (uint32_t)r * GS_BLOCK + threadIdx.x;
     if (idx < range.y) {
@@ -95,7 +128,7 @@ __device__ __forceinline__ void load_batch(const BlendParams &p, Batch &buf, uin
         buf.id[threadIdx.x] = vg;
         cp_async16(&buf.A[threadIdx.x], p.ws.recA + vg);
         cp_async16(&buf.B[threadIdx.x], p.ws.recB + vg);
-        if (p.rgb) cp_async16(&buf.C[threadIdx.x], p.ws.recC + vg);
+        if (RGB) cp_async16(&buf.C[threadIdx.x], p.ws.recC + vg);
     }
     cp_async_commit();
 }
@@ -115,10 +148,10 @@ __device__ __forceinline__ void warp_pixel(int tid, int tx, int ty, int &px, int
     sy1 = (float)(by + 3);
 }
 
-template <bool DEPTH>
-__global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
+template <bool DEPTH, bool RGB>
+__global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams p)
 {
-    __shared__ Batch sb[2];
+    __shared__ Batch<RGB> sb[2];
     __shared__ gsevt_view V;
     const int tile = blockIdx.x;
     if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
@@ -139,7 +172,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
     const int lane = threadIdx.x & 31;
     if (rounds > 0) load_batch(p, sb[0], range, 0);
     for (int r = 0; r < rounds; ++r) {
-        Batch &cur = sb[r & 1];
+        Batch<RGB> &cur = sb[r & 1];
         if (r + 1 < rounds) {
             load_batch(p, sb[(r + 1) & 1], range, r + 1);
             cp_async_wait<1>();
@@ -149,10 +182,10 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
         if (__syncthreads_count(done) == GS_BLOCK) break;
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
         if ((int)threadIdx.x < n) {
-            float th;
-            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &th);
-            if (DEPTH) cur.thr[threadIdx.x] = th;
-            else cur.A[threadIdx.x].z = th;  // depth is not needed: keep the threshold in its slot
+            float4 e;
+            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &e);
+            cur.ell[threadIdx.x] = e;
+            if (!DEPTH) cur.A[threadIdx.x].z = e.w;  // depth is not needed: keep the threshold in its slot
         }
         __syncthreads();
         bool warp_done = false;
@@ -162,6 +195,10 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
             if (c0 + lane < n) {
                 const float4 bx = cur.box[c0 + lane];
                 hit = bx.y >= sx0 && bx.x <= sx1 && bx.w >= sy0 && bx.z <= sy1;
+                if (hit) {
+                    const float4 A = cur.A[c0 + lane];
+                    hit = ellipse_hits(A.x, A.y, cur.ell[c0 + lane], sx0, sx1, sy0, sy1);
+                }
             }
             unsigned mask = __ballot_sync(0xffffffffu, hit);
             while (mask) {
@@ -173,12 +210,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
                 const float dx = A.x - pxf, dy = A.y - pyf;
                 const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
                 // power > 0, or below the Gaussian's alpha threshold (fails the alpha test anyway)
-                if (power > 0.0f || power < (DEPTH ? cur.thr[j] : A.z)) continue;
+                if (power > 0.0f || power < (DEPTH ? cur.ell[j].w : A.z)) continue;
                 const float alpha = fminf(0.99f, B.w * gs_expf(power));
                 if (alpha < 1.0f / 255.0f) continue;
                 const float test_T = T * (1.0f - alpha);
                 if (test_T < 0.0001f) { done = true; continue; }
-                if (p.rgb) {
+                if (RGB) {
                     const float4 Cc = cur.C[j];
                     C0 = C0 + (Cc.x * alpha) * T;
                     C1 = C1 + (Cc.y * alpha) * T;
@@ -199,7 +236,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_fwd(BlendParams p)
     if (inside) {
         const int pix = V.pix_offset + py * V.width + px;
         const size_t P = (size_t)p.total_pixels;
-        if (p.rgb) {
+        if (RGB) {
             p.image[pix] = C0 + T * V.bg[0];
             p.image[P + pix] = C1 + T * V.bg[1];
             p.image[2 * P + pix] = C2 + T * V.bg[2];
@@ -259,7 +296,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
 {
     constexpr bool RGB = MODE == 2;
     constexpr int NC = Comps<MODE>::n;
-    __shared__ Batch sb[2];
+    __shared__ Batch<RGB> sb[2];
     __shared__ float acc[GS_BLOCK][NC + 1];
     __shared__ gsevt_view V;
     const int tile = blockIdx.x;
@@ -323,7 +360,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
     bool done = !inside;
     if (rounds > 0) load_batch(p, sb[0], range, 0);
     for (int r = 0; r < rounds; ++r) {
-        Batch &cur = sb[r & 1];
+        Batch<RGB> &cur = sb[r & 1];
         if (r + 1 < rounds) {
             load_batch(p, sb[(r + 1) & 1], range, r + 1);
             cp_async_wait<1>();
@@ -333,10 +370,10 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         if (__syncthreads_count(done) == GS_BLOCK) break;
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
         if ((int)threadIdx.x < n) {
-            float th;
-            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &th);
-            if (MODE != 0) cur.thr[threadIdx.x] = th;
-            else cur.A[threadIdx.x].z = th;  // the tracker adjoint needs no depth
+            float4 e;
+            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &e);
+            cur.ell[threadIdx.x] = e;
+            if (MODE == 0) cur.A[threadIdx.x].z = e.w;  // the tracker adjoint needs no depth
         }
         __syncthreads();
         bool warp_done = false;
@@ -345,6 +382,10 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
             if (c0 + lane < n) {
                 const float4 bx = cur.box[c0 + lane];
                 hit = bx.y >= sx0 && bx.x <= sx1 && bx.w >= sy0 && bx.z <= sy1;
+                if (hit) {
+                    const float4 A = cur.A[c0 + lane];
+                    hit = ellipse_hits(A.x, A.y, cur.ell[c0 + lane], sx0, sx1, sy0, sy1);
+                }
             }
             unsigned mask = __ballot_sync(0xffffffffu, hit);
             while (mask) {
@@ -359,7 +400,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                     const float4 A = cur.A[j], B = cur.B[j];
                     const float dx = A.x - pxf, dy = A.y - pyf;
                     const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
-                    if (power <= 0.0f && !(power < (MODE != 0 ? cur.thr[j] : A.z))) {
+                    if (power <= 0.0f && !(power < (MODE != 0 ? cur.ell[j].w : A.z))) {
                         const float G = gs_expf(power);
                         const float araw = B.w * G;
                         const float alpha = fminf(0.99f, araw);
@@ -463,8 +504,14 @@ int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     if (f->L.total_tiles <= 0) return GSEVT_OK;
     BlendParams p = make_params(f, ws, vals);
     if (f->n_touched) cudaMemsetAsync(f->n_touched, 0, (size_t)f->L.num_vg * 4, s);
-    if (f->depth) k_blend_fwd<true><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
-    else k_blend_fwd<false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    const int n = f->L.total_tiles;
+    if (p.rgb) {
+        if (f->depth) k_blend_fwd<true, true><<<n, GS_BLOCK, 0, s>>>(p);
+        else k_blend_fwd<false, true><<<n, GS_BLOCK, 0, s>>>(p);
+    } else {
+        if (f->depth) k_blend_fwd<true, false><<<n, GS_BLOCK, 0, s>>>(p);
+        else k_blend_fwd<false, false><<<n, GS_BLOCK, 0, s>>>(p);
+    }
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }
