@@ -19,16 +19,35 @@
 
 template <typename KT>
 int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
-                     int bits, uint32_t max_keys, const Workspace &ws, int *out_buf, cudaStream_t s);
+                     int bits, uint32_t max_keys, int kpt, const Workspace &ws, int *out_buf, cudaStream_t s);
 
 namespace {
 
 // exclusive scan of n block sums (one block of 1024 threads); total into *total and an
 // overflow flag when the total exceeds `capacity` (0: no check)
+__device__ void scan_blocks(const uint32_t *sums, uint32_t *offs, int n, uint32_t *total, uint32_t *status,
+                            uint32_t capacity, unsigned long long *part);
 __global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t *sums, uint32_t *offs, int n, uint32_t *total,
                                                       uint32_t *status, uint32_t capacity)
 {
     __shared__ unsigned long long part[1024];
+    scan_blocks(sums, offs, n, total, status, capacity, part);
+}
+
+// two independent scans in one launch (the fine and the coarse pair counts)
+__global__ void __launch_bounds__(1024) k_scan_blocks2(const uint32_t *sums, uint32_t *offs, uint32_t *total,
+                                                       const uint32_t *sums2, uint32_t *offs2, uint32_t *total2,
+                                                       int n, uint32_t *status, uint32_t capacity)
+{
+    __shared__ unsigned long long part[1024];
+    scan_blocks(sums, offs, n, total, status, capacity, part);
+    __syncthreads();
+    scan_blocks(sums2, offs2, n, total2, status, capacity, part);
+}
+
+__device__ void scan_blocks(const uint32_t *sums, uint32_t *offs, int n, uint32_t *total, uint32_t *status,
+                            uint32_t capacity, unsigned long long *part)
+{
     int t = threadIdx.x;
     int per = (n + 1023) / 1024;
     int b = t * per, e = min(n, b + per);
@@ -118,22 +137,65 @@ __global__ void __launch_bounds__(GS_BLOCK) k_compact(BinParams p)
     }
 }
 
-// tiles touched per block of 256 depth-sorted visible slots
+// super-tile rectangle [sx0, sx1) x [sy0, sy1) of a tile rectangle (bin.y = x0 | y0 << 16,
+// bin.z = x1 | y1 << 16, exclusive upper bounds)
+__device__ __forceinline__ void super_rect(int4 bin, int &sx0, int &sy0, int &sx1, int &sy1)
+{
+    sx0 = (bin.y & 0xffff) / GS_SUPER;
+    sy0 = ((bin.y >> 16) & 0xffff) / GS_SUPER;
+    sx1 = ((bin.z & 0xffff) - 1) / GS_SUPER + 1;
+    sy1 = (((bin.z >> 16) & 0xffff) - 1) / GS_SUPER + 1;
+}
+
+// tiles touched per block of 256 depth-sorted visible slots; with COARSE also the
+// super-tiles touched (csums) and, in block 0, the first super-tile of every view (soffs)
+template <bool COARSE>
 __global__ void __launch_bounds__(GS_BLOCK) k_sorted_sums(BinParams p, const uint32_t *sorted_vals)
 {
-    __shared__ uint32_t wsum[GS_BLOCK / 32];
+    __shared__ uint32_t wsum[GS_BLOCK / 32], wsum2[GS_BLOCK / 32];
     const uint32_t nvis = p.ws.status[5];
     const uint32_t i = blockIdx.x * GS_BLOCK + threadIdx.x;
-    uint32_t cnt = 0;
-    if (i < nvis) cnt = (uint32_t)p.ws.bin[sorted_vals[i]].x;
+    uint32_t cnt = 0, scnt = 0;
+    if (i < nvis) {
+        const int4 b = p.ws.bin[sorted_vals[i]];
+        cnt = (uint32_t)b.x;
+        if (COARSE && cnt > 0) {
+            int sx0, sy0, sx1, sy1;
+            super_rect(b, sx0, sy0, sx1, sy1);
+            scnt = (uint32_t)((sx1 - sx0) * (sy1 - sy0));
+        }
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
+    for (int o = 16; o > 0; o >>= 1) {
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if (COARSE) scnt += __shfl_xor_sync(0xffffffffu, scnt, o);
+    }
+    if ((threadIdx.x & 31) == 0) { wsum[threadIdx.x >> 5] = cnt; wsum2[threadIdx.x >> 5] = scnt; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t t = 0;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) t += wsum[w];
+        uint32_t t = 0, t2 = 0;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) { t += wsum[w]; t2 += wsum2[w]; }
         p.ws.tsums[blockIdx.x] = t;
+        if (COARSE) p.ws.csums[blockIdx.x] = t2;
+    }
+    if (COARSE && blockIdx.x == 0) {
+        __syncthreads();
+        uint32_t carry = 0;
+        for (int v0 = 0; v0 < p.num_views; v0 += GS_BLOCK) {
+            const int v = v0 + (int)threadIdx.x;
+            uint32_t sv = 0;
+            if (v < p.num_views) {
+                const gsevt_view &V = p.views[v];
+                sv = (uint32_t)(((V.tiles_x + GS_SUPER - 1) / GS_SUPER) * ((V.tiles_y + GS_SUPER - 1) / GS_SUPER));
+            }
+            const uint32_t ex = block_excl_scan(sv, wsum);
+            if (v < p.num_views) p.ws.soffs[v] = carry + ex;
+            if (threadIdx.x == GS_BLOCK - 1) wsum2[0] = ex + sv;
+            __syncthreads();
+            carry += wsum2[0];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) p.ws.soffs[p.num_views] = carry;
     }
 }
 
@@ -201,9 +263,208 @@ __global__ void __launch_bounds__(GS_BLOCK) k_duplicate(BinParams p, const uint3
     }
 }
 
-__global__ void k_ranges(const uint32_t *keys, const uint32_t *status, uint32_t capacity, uint2 *ranges)
+// Coarse duplication for the batched tracker: in depth order, one (super-tile id, slot)
+// pair per 4x4-tile super-tile of the slot's rectangle (row-major), written with the same
+// warp-cooperative expansion as k_duplicate.
+__global__ void __launch_bounds__(GS_BLOCK) k_duplicate_coarse(BinParams p, const uint32_t *sorted_vals)
 {
-    uint32_t K = min(status[1], capacity);
+    __shared__ uint32_t wtot[GS_BLOCK / 32];
+    const uint32_t nvis = p.ws.status[5];
+    const uint32_t i = blockIdx.x * GS_BLOCK + threadIdx.x;
+    if (blockIdx.x * GS_BLOCK >= nvis) return;  // uniform per block
+    const int lane = threadIdx.x & 31;
+    uint32_t vg = 0;
+    int4 bin = make_int4(0, 0, 0, 0);
+    if (i < nvis) {
+        vg = sorted_vals[i];
+        bin = p.ws.bin[vg];
+    }
+    int sx0 = 0, sy0 = 0, srw = 1, soff = 0, stx = 1;
+    uint32_t cnt = 0;
+    if (bin.x > 0) {
+        p.ws.gradA[vg] = make_float4(0, 0, 0, 0);
+        p.ws.gradB[vg] = make_float4(0, 0, 0, 0);
+        if (p.rgb) p.ws.gradC[vg] = make_float4(0, 0, 0, 0);
+        const int v = find_view_by_vg(p.views, p.num_views, vg);
+        const gsevt_view &V = p.views[v];
+        int sx1, sy1;
+        super_rect(bin, sx0, sy0, sx1, sy1);
+        srw = sx1 - sx0;
+        cnt = (uint32_t)(srw * (sy1 - sy0));
+        soff = (int)p.ws.soffs[v];
+        stx = (V.tiles_x + GS_SUPER - 1) / GS_SUPER;
+    }
+    const uint32_t off = p.ws.coffs[blockIdx.x] + block_excl_scan(cnt, wtot);
+    uint32_t winc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, winc, o);
+        if (lane >= o) winc += y;
+    }
+    const uint32_t wex = winc - cnt;
+    const uint32_t wtotal = __shfl_sync(0xffffffffu, winc, 31);
+    const uint32_t wbase = __shfl_sync(0xffffffffu, off, 0);
+    for (uint32_t c = 0; c < wtotal; c += 32) {
+        const uint32_t k = c + lane;
+        int s = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const uint32_t e = __shfl_sync(0xffffffffu, wex, s + step);
+            if (e <= k) s += step;
+        }
+        const uint32_t q = k - __shfl_sync(0xffffffffu, wex, s);
+        const int ssx0 = __shfl_sync(0xffffffffu, sx0, s), ssy0 = __shfl_sync(0xffffffffu, sy0, s);
+        const int ssrw = __shfl_sync(0xffffffffu, srw, s), ssoff = __shfl_sync(0xffffffffu, soff, s);
+        const int sstx = __shfl_sync(0xffffffffu, stx, s);
+        const uint32_t svg = __shfl_sync(0xffffffffu, vg, s);
+        const uint32_t idx = wbase + k;
+        if (k < wtotal && idx < p.capacity) {
+            const int y = ssy0 + (int)(q / (uint32_t)ssrw), x = ssx0 + (int)(q % (uint32_t)ssrw);
+            p.ws.keys[0][idx] = (uint32_t)(ssoff + y * sstx + x);
+            p.ws.vals[0][idx] = svg;
+        }
+    }
+}
+
+// Tiles of super-tile (sx, sy) covered by a tile rectangle, as a 16-bit mask (bit
+// 4 ly + lx for local tile (lx, ly)).
+__device__ __forceinline__ uint32_t cover_mask(uint32_t lo, uint32_t hi, int X, int Y)
+{
+    const int x0 = max((int)(lo & 0xffff) - X, 0), x1 = min((int)(hi & 0xffff) - X, GS_SUPER);
+    const int y0 = max((int)(lo >> 16) - Y, 0), y1 = min((int)(hi >> 16) - Y, GS_SUPER);
+    if (x0 >= x1 || y0 >= y1) return 0u;
+    const uint32_t row = ((1u << x1) - 1u) & ~((1u << x0) - 1u);
+    uint32_t m = 0;
+#pragma unroll
+    for (int ly = 0; ly < GS_SUPER; ++ly)
+        if (ly >= y0 && ly < y1) m |= row << (GS_SUPER * ly);
+    return m;
+}
+
+// One block per super-tile (32 warps); warp w takes the w-th contiguous 32nd of the
+// super-tile's depth-ordered coarse list, four groups of 32 entries at a time (their
+// loads in flight together).  Pass 1 counts, per warp and tile, the entries whose
+// rectangle covers the tile (one ballot per tile per group); the block then claims a
+// contiguous region of the fine list with one atomic add and lays its 16 tile lists out
+// in it; pass 2 rescans the same entries and writes each one into the lists of the tiles
+// it covers, at (tile start + earlier warps' count + running count + rank in the ballot).
+// Order within a tile is the coarse list order, i.e. depth order with ties in slot order
+// - the order of the full stable (tile | depth) sort.  Tile ranges are written for every
+// tile of the super-tile; their placement in the fine list follows the order in which
+// blocks claim regions, which does not affect any tile's content.
+#define FILTER_TILES (GS_SUPER * GS_SUPER)
+#define FILTER_WARPS 32
+#define FILTER_ILP 4
+__device__ __forceinline__ void filter_load(const uint32_t *cvals, const int4 *bin, uint32_t g, uint32_t b1,
+                                            int lane, int X, int Y, uint32_t (&vg)[FILTER_ILP],
+                                            uint32_t (&m)[FILTER_ILP])
+{
+#pragma unroll
+    for (int k = 0; k < FILTER_ILP; ++k) {
+        const uint32_t i = g + 32 * k + lane;
+        vg[k] = i < b1 ? cvals[i] : 0xffffffffu;
+    }
+#pragma unroll
+    for (int k = 0; k < FILTER_ILP; ++k) {
+        m[k] = 0;
+        if (vg[k] != 0xffffffffu) {
+            const int4 b = bin[vg[k]];
+            m[k] = cover_mask((uint32_t)b.y, (uint32_t)b.z, X, Y);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(FILTER_WARPS * 32) k_filter_tiles(const gsevt_view *views, int num_views,
+                                                                  Workspace ws, const uint32_t *cvals,
+                                                                  uint32_t *fine_vals, uint32_t capacity)
+{
+    __shared__ uint32_t s_cnt[FILTER_WARPS][FILTER_TILES + 1];  // [warp][tile]
+    __shared__ uint32_t s_start[FILTER_TILES];
+    const uint32_t sid = blockIdx.x;
+    if (sid >= ws.soffs[num_views]) return;  // uniform per block
+    int lo = 0, hi = num_views - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (ws.soffs[mid] <= sid) lo = mid; else hi = mid - 1;
+    }
+    const gsevt_view &V = views[lo];
+    const int stx = (V.tiles_x + GS_SUPER - 1) / GS_SUPER;
+    const uint32_t local = sid - ws.soffs[lo];
+    const int X = (int)(local % (uint32_t)stx) * GS_SUPER, Y = (int)(local / (uint32_t)stx) * GS_SUPER;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint2 sr = ws.sranges[sid];
+    const uint32_t len = sr.y - sr.x, seg = (len + FILTER_WARPS - 1) / FILTER_WARPS;
+    const uint32_t b0 = sr.x + min(len, (uint32_t)w * seg), b1 = sr.x + min(len, (uint32_t)(w + 1) * seg);
+    const uint32_t lt = (1u << lane) - 1u;
+
+    // pass 1: per-tile counts of this warp's entries (lane t holds tile t's count)
+    uint32_t cnt = 0;
+    for (uint32_t g = b0; g < b1; g += 32 * FILTER_ILP) {
+        uint32_t vg[FILTER_ILP], m[FILTER_ILP];
+        filter_load(cvals, ws.bin, g, b1, lane, X, Y, vg, m);
+#pragma unroll
+        for (int k = 0; k < FILTER_ILP; ++k) {
+#pragma unroll
+            for (int t = 0; t < FILTER_TILES; ++t) {
+                const uint32_t bal = __ballot_sync(0xffffffffu, (m[k] >> t) & 1u);
+                if (lane == t) cnt += __popc(bal);
+            }
+        }
+    }
+    if (lane < FILTER_TILES) s_cnt[w][lane] = cnt;
+    __syncthreads();
+    // per tile: exclusive prefix over warps; tile totals -> region of this super-tile
+    if (w == 0) {
+        uint32_t tot = 0;
+        if (lane < FILTER_TILES) {
+            for (int q = 0; q < FILTER_WARPS; ++q) {
+                const uint32_t c = s_cnt[q][lane];
+                s_cnt[q][lane] = tot;
+                tot += c;
+            }
+        }
+        uint32_t inc = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        uint32_t base = 0;
+        if (lane == FILTER_TILES - 1) base = atomicAdd(ws.status + 7, inc);
+        base = __shfl_sync(0xffffffffu, base, FILTER_TILES - 1);
+        if (lane < FILTER_TILES) {
+            const uint32_t start = base + inc - tot;
+            s_start[lane] = start;
+            const int tx = X + (lane % GS_SUPER), ty = Y + (lane / GS_SUPER);
+            if (tx < V.tiles_x && ty < V.tiles_y)
+                ws.ranges[V.tile_offset + ty * V.tiles_x + tx] = make_uint2(start, start + tot);
+        }
+    }
+    __syncthreads();
+    // pass 2: write (starts and running counts are warp-uniform)
+    uint32_t pos[FILTER_TILES];
+#pragma unroll
+    for (int t = 0; t < FILTER_TILES; ++t) pos[t] = s_start[t] + s_cnt[w][t];
+    for (uint32_t g = b0; g < b1; g += 32 * FILTER_ILP) {
+        uint32_t vg[FILTER_ILP], m[FILTER_ILP];
+        filter_load(cvals, ws.bin, g, b1, lane, X, Y, vg, m);
+#pragma unroll
+        for (int k = 0; k < FILTER_ILP; ++k) {
+#pragma unroll
+            for (int t = 0; t < FILTER_TILES; ++t) {
+                const bool hit = (m[k] >> t) & 1u;
+                const uint32_t bal = __ballot_sync(0xffffffffu, hit);
+                const uint32_t at = pos[t] + __popc(bal & lt);
+                if (hit && at < capacity) fine_vals[at] = vg[k];
+                pos[t] += __popc(bal);
+            }
+        }
+    }
+}
+
+__global__ void k_ranges(const uint32_t *keys, const uint32_t *count_word, uint32_t capacity, uint2 *ranges)
+{
+    uint32_t K = min(*count_word, capacity);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
         uint32_t t = keys[i];
         if (i == 0 || keys[i - 1] != t) ranges[t].x = i;
@@ -227,13 +488,14 @@ BinParams make_params(const gsevt_frame *f, const Workspace &ws)
 
 // After preprocess: visible-slot compaction, depth sort, key offsets in depth order.
 // Leaves the key count in status[1] (and flags overflow) and N_vis in status[5].
-int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s)
+int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s, bool coarse)
 {
     const gsevt_layout &L = f->L;
     const uint32_t nb = gs_sorted_blocks(L);
     if (L.num_scan_blocks <= 0 || L.num_vg <= 0) {
         cudaMemsetAsync(ws.status + 1, 0, 4, s);
         cudaMemsetAsync(ws.status + 5, 0, 4, s);
+        cudaMemsetAsync(ws.status + 6, 0, 4, s);
         GS_CUDA_CHECK();
         return GSEVT_OK;
     }
@@ -244,11 +506,18 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
     int buf = 0;
     uint32_t *dk[2] = {ws.dkeys[0], ws.dkeys[1]};
     uint32_t *dv[2] = {ws.dvals[0], ws.dvals[1]};
-    int st = gs_launch_sort_t<uint32_t>(dk, dv, ws.status + 5, (uint32_t)L.num_vg, 32, (uint32_t)L.num_vg, ws, &buf, s);
+    int st = gs_launch_sort_t<uint32_t>(dk, dv, ws.status + 5, (uint32_t)L.num_vg, 32, (uint32_t)L.num_vg,
+                                       GS_SORT_KPT_DEPTH, ws, &buf, s);
     if (st) return st;
     if (buf != 0) return GSEVT_ERR_ARG;  // 4 passes: the result is back in buffer 0
-    k_sorted_sums<<<nb, GS_BLOCK, 0, s>>>(p, ws.dvals[0]);
-    k_scan_blocks<<<1, 1024, 0, s>>>(ws.tsums, ws.toffs, (int)nb, ws.status + 1, ws.status, L.key_capacity);
+    if (coarse) {
+        k_sorted_sums<true><<<nb, GS_BLOCK, 0, s>>>(p, ws.dvals[0]);
+        k_scan_blocks2<<<1, 1024, 0, s>>>(ws.tsums, ws.toffs, ws.status + 1, ws.csums, ws.coffs, ws.status + 6,
+                                          (int)nb, ws.status, L.key_capacity);
+    } else {
+        k_sorted_sums<false><<<nb, GS_BLOCK, 0, s>>>(p, ws.dvals[0]);
+        k_scan_blocks<<<1, 1024, 0, s>>>(ws.tsums, ws.toffs, (int)nb, ws.status + 1, ws.status, L.key_capacity);
+    }
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }
@@ -266,11 +535,50 @@ int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, 
     int buf = 0;
     uint32_t *k[2] = {ws.keys[0], ws.keys[1]};
     uint32_t *v[2] = {ws.vals[0], ws.vals[1]};
-    int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 1, L.key_capacity, gs_tile_bits(L), max_keys, ws, &buf, s);
+    int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 1, L.key_capacity, gs_tile_bits(L), max_keys,
+                                       GS_SORT_KPT_TILES, ws, &buf, s);
     if (st) return st;
     if (buf != gs_tile_sort_buffer(L)) return GSEVT_ERR_ARG;
     int blocks = (int)std::min<uint32_t>((max_keys + 255) / 256, 152u * 16u);
-    k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status, L.key_capacity, ws.ranges);
+    k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status + 1, L.key_capacity, ws.ranges);
     GS_CUDA_CHECK();
+    return GSEVT_OK;
+}
+
+// Batched-tracker binning through 4x4-tile super-tiles (after gs_launch_depth_order with
+// coarse = true): coarse duplication in depth order, stable sort of the coarse pairs by
+// super-tile, super-tile ranges, and the per-super-tile filter that writes the fine
+// lists and the tile ranges.  The fine lists and ranges equal those of
+// gs_launch_bin (depth order within a tile, ties in slot order); only the values are
+// produced (the blend reads no keys).  The fine list is returned through *fine_vals.
+int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, uint32_t **fine_vals,
+                         cudaStream_t s)
+{
+    const gsevt_layout &L = f->L;
+    *fine_vals = ws.vals[0];
+    const uint32_t nsup = gs_super_bound(L);
+    cudaMemsetAsync(ws.sranges, 0, (size_t)nsup * 8, s);
+    cudaMemsetAsync(ws.status + 7, 0, 4, s);  // fine-list region cursor
+    GS_CUDA_CHECK();
+    if (L.num_vg <= 0 || max_keys == 0 || L.total_tiles <= 0) {
+        cudaMemsetAsync(ws.ranges, 0, (size_t)L.total_tiles * sizeof(uint2), s);
+        GS_CUDA_CHECK();
+        return GSEVT_OK;
+    }
+    BinParams p = make_params(f, ws);
+    k_duplicate_coarse<<<gs_sorted_blocks(L), GS_BLOCK, 0, s>>>(p, ws.dvals[0]);
+    GS_CUDA_CHECK();
+    int buf = 0;
+    uint32_t *k[2] = {ws.keys[0], ws.keys[1]};
+    uint32_t *v[2] = {ws.vals[0], ws.vals[1]};
+    int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 6, L.key_capacity, gs_super_bits(L), max_keys,
+                                        GS_SORT_KPT_TILES, ws, &buf, s);
+    if (st) return st;
+    int blocks = (int)std::min<uint32_t>((max_keys + 255) / 256, 152u * 16u);
+    k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status + 6, L.key_capacity, ws.sranges);
+    k_filter_tiles<<<nsup, FILTER_WARPS * 32, 0, s>>>(f->views, L.num_views, ws, ws.vals[buf], ws.vals[buf ^ 1],
+                                                     L.key_capacity);
+    GS_CUDA_CHECK();
+    *fine_vals = ws.vals[buf ^ 1];
     return GSEVT_OK;
 }

@@ -6,8 +6,11 @@
 
 int gs_launch_preprocess_fwd(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
 int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gsevt_map_grads *grads_dev,
-                             double *xi_out, cudaStream_t s);
-int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
+                             double *xi_out, cudaStream_t s,
+                             bool reduce);
+int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s, bool coarse);
+int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, uint32_t **fine_vals,
+                         cudaStream_t s);
 int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, cudaStream_t s);
 int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s);
 int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, const float *dL_dimage,
@@ -81,7 +84,8 @@ extern "C" void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out)
                                        w.vis_sums, w.vis_offs, w.dkeys[0], w.dkeys[1], w.dvals[0], w.dvals[1],
                                        w.tsums, w.toffs, w.keys[0], w.keys[1], w.vals[0], w.vals[1], w.sort_hist,
                                        w.sort_counter, w.sort_lookback, w.ranges, w.loss_part, w.loss_scal,
-                                       w.loss_done, w.xi_part, w.xi};
+                                       w.loss_done, w.xi_part, w.xi, w.csums, w.coffs, w.soffs,
+                                       w.sranges};
     for (int i = 0; i < GS_WS_REGIONS; ++i)
         out[i] = ptrs[i] ? (uint64_t)((const char *)ptrs[i] - base) : UINT64_MAX;
 }
@@ -118,7 +122,7 @@ extern "C" int gsevt_preprocess_fwd(const gsevt_frame *f, gsevt_stream_t stream)
     GS_CUDA_CHECK();
     st = gs_launch_preprocess_fwd(f, ws, s);
     if (st) return st;
-    return gs_launch_depth_order(f, ws, s);
+    return gs_launch_depth_order(f, ws, s, false);
 }
 
 extern "C" int gsevt_bin_and_sort(const gsevt_frame *f, uint32_t max_keys, gsevt_stream_t stream)
@@ -175,7 +179,7 @@ extern "C" int gsevt_preprocess_bwd(const gsevt_frame *f, double *xi_out, const 
             cudaSuccess)
             return GSEVT_ERR_CUDA;
     }
-    return gs_launch_preprocess_bwd(f, ws, dev_tab, xi_out, s);
+    return gs_launch_preprocess_bwd(f, ws, dev_tab, xi_out, s, true);
 }
 
 extern "C" int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *poses, int32_t num_poses,
@@ -186,11 +190,16 @@ extern "C" int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *
     if (st) return st;
     if (!poses || num_poses <= 0 || !f->pairs || f->L.num_pairs <= 0 || f->L.channels != 1) return GSEVT_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    if ((st = gsevt_preprocess_fwd(f, stream))) return st;
-    if ((st = gsevt_bin_and_sort(f, 0, stream))) return st;
-    if ((st = gs_launch_blend_fwd(f, ws, ws.vals[sorted_buffer(f)], s))) return st;
+    // binning through super-tiles: the same per-tile lists as gsevt_bin_and_sort
+    cudaMemsetAsync(ws.status, 0, 8, s);
+    GS_CUDA_CHECK();
+    if ((st = gs_launch_preprocess_fwd(f, ws, s))) return st;
+    if ((st = gs_launch_depth_order(f, ws, s, true))) return st;
+    uint32_t *fine = nullptr;
+    if ((st = gs_launch_bin_coarse(f, ws, f->L.key_capacity, &fine, s))) return st;
+    if ((st = gs_launch_blend_fwd(f, ws, fine, s))) return st;
     if ((st = gs_launch_loss(f, ws, loss_out, s))) return st;
-    if ((st = gs_launch_blend_bwd(f, ws, ws.vals[sorted_buffer(f)], nullptr, nullptr, nullptr, s))) return st;
-    if ((st = gs_launch_preprocess_bwd(f, ws, nullptr, nullptr, s))) return st;
+    if ((st = gs_launch_blend_bwd(f, ws, fine, nullptr, nullptr, nullptr, s))) return st;
+    if ((st = gs_launch_preprocess_bwd(f, ws, nullptr, nullptr, s, false))) return st;
     return gs_launch_track_finalize(f, ws, poses, num_poses, loss_out, s);
 }

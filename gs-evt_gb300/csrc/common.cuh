@@ -14,8 +14,13 @@
 #include "gsevt.h"
 
 #define GS_BLOCK 256
-#define GS_SORT_KPT 12
-#define GS_SORT_TILE (GS_BLOCK * GS_SORT_KPT)
+// keys per thread of a sort pass (template instances 4, 8 and 12 exist)
+#ifndef GS_SORT_KPT_TILES
+#define GS_SORT_KPT_TILES 12
+#endif
+#ifndef GS_SORT_KPT_DEPTH
+#define GS_SORT_KPT_DEPTH 12
+#endif
 #define GS_MAX_PASSES 8
 #define GS_SPIN_LIMIT (1u << 22)
 
@@ -52,7 +57,8 @@ __host__ __device__ __forceinline__ float gs_expf(float x)
 // ------------------------------------------------------------ workspace ---------
 struct Workspace {
     uint32_t *status;     // [0] status bits, [1] num keys, [2] last sort epoch, [4] sort epoch base,
-                          // [5] number of visible (view, Gaussian) slots
+                          // [5] number of visible (view, Gaussian) slots, [6] number of coarse
+                          // (super-tile, slot) pairs, [7] fine-list region cursor
     int4 *bin;            // [num_vg] {touched, rect lo (x0 | y0<<16), rect hi, depth bits}
     float4 *recA;         // [num_vg] {mean x, mean y, depth, grey}
     float4 *recB;         // [num_vg] {conic x, y, z, opacity}
@@ -77,22 +83,39 @@ struct Workspace {
     uint32_t *loss_done;  // [num_pairs]
     double *xi_part;      // [num_scan_blocks][6]
     double *xi;           // [num_views][6]
+    // super-tile binning (batched tracker): 4x4-tile super-tiles, numbered per view
+    uint32_t *csums;      // [sorted blocks] super-tiles touched per block of depth-sorted slots
+    uint32_t *coffs;      // [sorted blocks]
+    uint32_t *soffs;      // [num_views + 1] first super-tile of each view; [num_views] = total
+    uint2 *sranges;       // [gs_super_bound] [start, end) of every super-tile in the sorted coarse pairs
     size_t bytes;
 };
 
-#define GS_WS_REGIONS 29
+#define GS_WS_REGIONS 33
+#define GS_SUPER 4   // tiles per super-tile side
 
 __host__ __device__ inline size_t gs_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
-inline uint32_t gs_sort_tiles(uint32_t cap) { return (cap + GS_SORT_TILE - 1) / GS_SORT_TILE; }
+inline uint32_t gs_sort_tiles(uint32_t cap, int kpt) { return (cap + GS_BLOCK * kpt - 1) / (GS_BLOCK * kpt); }
 inline uint32_t gs_sorted_blocks(const gsevt_layout &L) { return ((uint32_t)(L.num_vg > 0 ? L.num_vg : 1) + GS_BLOCK - 1) / GS_BLOCK; }
 inline uint32_t gs_lookback_tiles(const gsevt_layout &L)
 {
     uint32_t cap = L.key_capacity > 0 ? L.key_capacity : 1;
     uint32_t vg = L.num_vg > 0 ? (uint32_t)L.num_vg : 1;
-    return gs_sort_tiles(cap > vg ? cap : vg);
+    return std::max(gs_sort_tiles(cap, GS_SORT_KPT_TILES), gs_sort_tiles(vg, GS_SORT_KPT_DEPTH));
 }
 inline int gs_tile_bits(const gsevt_layout &L) { return L.sort_bits - 32; }
+// upper bound on the number of super-tiles: ceil(tx/4) ceil(ty/4) <= floor(tx ty / 4) + 1 per view
+inline uint32_t gs_super_bound(const gsevt_layout &L)
+{
+    return (uint32_t)(L.total_tiles > 0 ? L.total_tiles : 0) / 4 + (uint32_t)(L.num_views > 0 ? L.num_views : 0) + 1;
+}
+inline int gs_super_bits(const gsevt_layout &L)
+{
+    uint32_t n = gs_super_bound(L), b = 1;
+    while ((1u << b) < n && b < 31) ++b;
+    return (int)b;
+}
 inline int gs_tile_sort_buffer(const gsevt_layout &L) { return ((gs_tile_bits(L) + 7) / 8) & 1; }
 
 // Carves the workspace in a fixed order; with base == nullptr it only sizes it.
@@ -138,6 +161,10 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     w.loss_done = (uint32_t *)take((size_t)L.num_pairs * 4);
     w.xi_part = (double *)take((size_t)L.num_scan_blocks * 6 * 8);
     w.xi = (double *)take((size_t)L.num_views * 6 * 8);
+    w.csums = (uint32_t *)take((size_t)gs_sorted_blocks(L) * 4);
+    w.coffs = (uint32_t *)take((size_t)gs_sorted_blocks(L) * 4);
+    w.soffs = (uint32_t *)take((size_t)(L.num_views + 1) * 4);
+    w.sranges = (uint2 *)take((size_t)gs_super_bound(L) * 8);
     w.bytes = off;
     return w;
 }

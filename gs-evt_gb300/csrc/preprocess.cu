@@ -634,8 +634,10 @@ int gs_launch_preprocess_fwd(const gsevt_frame *f, const Workspace &ws, cudaStre
     return GSEVT_OK;
 }
 
+// reduce = false leaves the per-view sums to the caller (the batched tracker's finalize
+// kernel reduces the partials itself)
 int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gsevt_map_grads *grads_dev,
-                             double *xi_out, cudaStream_t s)
+                             double *xi_out, cudaStream_t s, bool reduce)
 {
     BwdParams p;
     p.views = f->views;
@@ -649,7 +651,7 @@ int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gs
         else k_preprocess_bwd<false><<<f->L.preprocess_blocks, GS_BLOCK, 0, s>>>(p);
         GS_CUDA_CHECK();
     }
-    k_xi_reduce<<<f->L.num_views, GS_BLOCK, 0, s>>>(f->views, f->maps, ws, f->L.num_views, xi_out);
+    if (reduce) k_xi_reduce<<<f->L.num_views, GS_BLOCK, 0, s>>>(f->views, f->maps, ws, f->L.num_views, xi_out);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

@@ -5,10 +5,12 @@
 // every pass; each pass is then a single kernel in which a block
 //   1. takes a tile ticket from an atomic counter (tickets are handed out in launch
 //      order, so every earlier tile belongs to a block that is already running),
-//   2. ranks its GS_SORT_TILE keys stably with warp-level match/ballot multisplit,
+//   2. ranks its 256 x KPT keys stably with warp-level match/ballot multisplit,
 //   3. publishes its per-digit counts to a look-back table and walks back over the
 //      earlier tiles (decoupled look-back) to get its exclusive per-digit prefix,
 //   4. scatters keys and values through shared memory to their global positions.
+// A pass whose digit is constant over all keys (its histogram holds every key in one
+// bin) is the identity permutation and runs as a plain copy.
 // Look-back entries are single 64-bit words {epoch:32 | flag:2 | count:30}; the epoch
 // changes every pass, so the table never needs clearing between passes or sorts (it
 // must be zero-filled once, when the workspace is created).  Every wait on a
@@ -19,15 +21,20 @@
 
 namespace {
 
-#define SORT_KPT GS_SORT_KPT
-#define SORT_TILE GS_SORT_TILE
 #define FLAG_AGG 1ull
 #define FLAG_PREFIX 2ull
 
 template <typename KT>
-__global__ void k_sort_hist(const KT *keys, const uint32_t *count, uint32_t capacity, int passes, uint32_t *hist)
+__global__ void k_sort_hist(const KT *keys, const uint32_t *count, uint32_t capacity, int passes, uint32_t *hist,
+                            uint32_t *status)
 {
     __shared__ uint32_t sh[GS_MAX_PASSES][256];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // epochs of this sort's passes: status[2] last epoch used, status[4] first epoch
+        const uint32_t e = status[2];
+        status[4] = e + 1;
+        status[2] = e + (uint32_t)passes;
+    }
     for (int i = threadIdx.x; i < GS_MAX_PASSES * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     uint32_t K = min(*count, capacity);
@@ -42,13 +49,6 @@ __global__ void k_sort_hist(const KT *keys, const uint32_t *count, uint32_t capa
     }
 }
 
-__global__ void k_sort_epoch(uint32_t *status, int passes)
-{
-    // status[2]: last epoch used; status[4]: first epoch of this sort
-    uint32_t e = status[2];
-    status[4] = e + 1;
-    status[2] = e + (uint32_t)passes;
-}
 
 template <typename KT>
 struct PassParams {
@@ -65,9 +65,10 @@ struct PassParams {
     int pass;
 };
 
-template <typename KT>
+template <typename KT, int SORT_KPT>
 __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
 {
+    constexpr uint32_t SORT_TILE = GS_BLOCK * SORT_KPT;
     __shared__ KT skeys[SORT_TILE];
     __shared__ uint32_t svals[SORT_TILE];
     __shared__ uint32_t whist[GS_BLOCK / 32][256];
@@ -77,12 +78,37 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
     __shared__ uint32_t wscan[GS_BLOCK / 32];
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const uint32_t K = min(*p.count, p.capacity);
+    const uint32_t ntiles = (K + SORT_TILE - 1) / SORT_TILE;
+    // A pass whose digit is the same for every key is the identity permutation of a
+    // stable sort: copy keys and values, with no ranking or look-back.
+    if (__syncthreads_or(p.hist[tid] == K)) {
+        const uint32_t stride = gridDim.x * GS_BLOCK;
+        for (uint32_t i0 = blockIdx.x * GS_BLOCK + tid; i0 < K; i0 += 4 * stride) {
+            KT kk[4];
+            uint32_t vv[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t i = i0 + k * stride;
+                if (i < K) { kk[k] = p.kin[i]; vv[k] = p.vin[i]; }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t i = i0 + k * stride;
+                if (i < K) { p.kout[i] = kk[k]; p.vout[i] = vv[k]; }
+            }
+        }
+        return;
+    }
+    // Persistent over tiles: a block takes the next ticket after finishing its tile, so a
+    // grid sized for the resident blocks covers any key count; every ticket below a
+    // block's own belongs to a running or finished block, so look-back never waits on a
+    // block that has not started.
+    for (;;) {
     if (tid == 0) s_tile = atomicAdd(p.counter, 1u);
     for (int i = tid; i < (GS_BLOCK / 32) * 256; i += GS_BLOCK) (&whist[0][0])[i] = 0;
     __syncthreads();
-    const uint32_t K = min(*p.count, p.capacity);
     const uint32_t tile = s_tile;
-    const uint32_t ntiles = (K + SORT_TILE - 1) / SORT_TILE;
     if (tile >= ntiles) return;
     const uint32_t base = tile * SORT_TILE;
     const uint32_t count = min((uint32_t)SORT_TILE, K - base);
@@ -184,6 +210,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
         p.kout[pos] = kk;
         p.vout[pos] = svals[i];
     }
+    __syncthreads();  // shared memory is reused by the next tile
+    }
 }
 
 }  // namespace
@@ -191,11 +219,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
 // Sorts keys[0]/vals[0] (count in *count, a device word) on the low `bits` bits; the
 // result is in buffer index (passes & 1), returned through *out_buf.  max_keys bounds
 // the grid (a host-known count, or the capacity when the count is only known on the
-// device).  The look-back table must hold gs_sort_tiles(capacity) * 256 entries.
+// device).  The look-back table must hold gs_sort_tiles(capacity, kpt) * 256 entries.
 template <typename KT>
 int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
-                     int bits, uint32_t max_keys, const Workspace &ws, int *out_buf, cudaStream_t s)
+                     int bits, uint32_t max_keys, int kpt, const Workspace &ws, int *out_buf, cudaStream_t s)
 {
+    if (kpt != 4 && kpt != 8 && kpt != 12) return GSEVT_ERR_ARG;
     int passes = (bits + 7) / 8;
     if (passes < 1) passes = 1;
     if (passes > GS_MAX_PASSES || passes * 8 > (int)(8 * sizeof(KT)) + 7) return GSEVT_ERR_ARG;
@@ -206,10 +235,11 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
     cudaMemsetAsync(ws.sort_counter, 0, GS_MAX_PASSES * 4, s);
     GS_CUDA_CHECK();
     int hblocks = (int)std::min<uint32_t>((max_keys + 1023) / 1024, 152u * 4u);
-    k_sort_hist<KT><<<hblocks, 256, 0, s>>>(keys[0], count, capacity, passes, ws.sort_hist);
-    k_sort_epoch<<<1, 1, 0, s>>>(ws.status, passes);
+    k_sort_hist<KT><<<hblocks, 256, 0, s>>>(keys[0], count, capacity, passes, ws.sort_hist, ws.status);
     GS_CUDA_CHECK();
-    uint32_t tiles = (max_keys + SORT_TILE - 1) / SORT_TILE;
+    // resident blocks per SM of the pass kernel (registers / shared memory bound)
+    const uint32_t per_sm = kpt == 4 ? 6u : (kpt == 8 ? 4u : 3u);
+    uint32_t tiles = std::min(gs_sort_tiles(max_keys, kpt), 152u * per_sm);
     for (int pass = 0; pass < passes; ++pass) {
         PassParams<KT> p;
         int src = pass & 1;
@@ -224,12 +254,14 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
         p.count = count;
         p.capacity = capacity;
         p.pass = pass;
-        k_sort_pass<KT><<<tiles, GS_BLOCK, 0, s>>>(p);
+        if (kpt == 4) k_sort_pass<KT, 4><<<tiles, GS_BLOCK, 0, s>>>(p);
+        else if (kpt == 8) k_sort_pass<KT, 8><<<tiles, GS_BLOCK, 0, s>>>(p);
+        else k_sort_pass<KT, 12><<<tiles, GS_BLOCK, 0, s>>>(p);
         GS_CUDA_CHECK();
     }
     return GSEVT_OK;
 }
 
 template int gs_launch_sort_t<uint32_t>(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_t *count,
-                                        uint32_t capacity, int bits, uint32_t max_keys, const Workspace &ws,
-                                        int *out_buf, cudaStream_t s);
+                                        uint32_t capacity, int bits, uint32_t max_keys, int kpt,
+                                        const Workspace &ws, int *out_buf, cudaStream_t s);

@@ -175,137 +175,210 @@ __device__ inline void write_view_pose(gsevt_view *V, const double *R, const dou
         V->campos[i] = (float)(-(R[i] * t[0] + R[3 + i] * t[1] + R[6 + i] * t[2]));
 }
 
-__global__ void k_track_finalize(gsevt_view *views, gsevt_pose_state *poses, int num_poses, Workspace ws,
-                                 const double *loss, gsevt_pair *pairs, int num_pairs)
+// One block per pose.  The block sums the per-scan-block twist partials of the pose's two
+// views (FP64; thread i adds partials i, i + 256, ... in order, four loads in flight, then
+// warp and block sums in a fixed order - the order of k_xi_reduce), with the pose state
+// staged in shared memory.  Warp 0 then runs the serial part with its lanes sharing the
+// independent pieces: the two views' chain terms (lanes 0, 1), the four Adam groups
+// (lanes 0-3), the pose update (lane 0) and the two view rewrites (lanes 0, 1).
+__global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, const gsevt_map *maps,
+                                                             gsevt_pose_state *poses, int num_poses, Workspace ws,
+                                                             const double *loss, gsevt_pair *pairs, int num_pairs)
 {
-    int pi = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double part[2][GS_BLOCK / 32][6];
+    __shared__ gsevt_pose_state S;
+    __shared__ float s_g[2][6], s_acc[2][12], s_grad[12], s_delta[12];
+    __shared__ int s_ok;
+    constexpr int WORDS = (int)(sizeof(gsevt_pose_state) / 4);
+    const int pi = blockIdx.x;
     if (pi >= num_poses) return;
-    gsevt_pose_state &S = poses[pi];
-    if (S.control && S.frozen) return;  // this problem's level is finished
-    const float h = (float)(S.delta_tau * 0.5);
-    float gpose[6] = {0, 0, 0, 0, 0, 0}, gvel[6] = {0, 0, 0, 0, 0, 0};
+    if (poses[pi].control && poses[pi].frozen) return;  // this problem's level is finished (uniform)
+    for (int i = threadIdx.x; i < WORDS; i += GS_BLOCK)
+        ((uint32_t *)&S)[i] = ((const uint32_t *)(poses + pi))[i];
+    __syncthreads();
     const int vids[2] = {S.last_view, S.next_view};
-    const float sg[2] = {-1.0f, 1.0f};
     for (int k = 0; k < 2; ++k) {
+        const gsevt_view &V = views[vids[k]];
+        const int nb = (maps[V.map].n + GS_BLOCK - 1) / GS_BLOCK;
+        const double *xp = ws.xi_part + (size_t)V.sb_offset * 6;
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int i0 = threadIdx.x; i0 < nb; i0 += 4 * GS_BLOCK) {
+            double x[4][6];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int i = i0 + j * GS_BLOCK;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) x[j][q] = i < nb ? xp[(size_t)i * 6 + q] : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) acc[q] += x[j][q];
+        }
+        for (int q = 0; q < 6; ++q) {
+            const double sm = warp_sum_d(acc[q]);
+            if ((threadIdx.x & 31) == 0) part[k][threadIdx.x >> 5][q] = sm;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        const int k = threadIdx.x / 6, q = threadIdx.x % 6;
+        double sm = 0;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) sm += part[k][w][q];
+        ws.xi[6 * vids[k] + q] = sm;
+        s_g[k][q] = (float)sm;
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    const float h = (float)(S.delta_tau * 0.5);
+    const float sg[2] = {-1.0f, 1.0f};
+    // chain of each view's twist gradient (lane k: view k)
+    if (lane < 2) {
+        const int k = lane;
         float g[6];
-        for (int i = 0; i < 6; ++i) g[i] = (float)ws.xi[6 * vids[k] + i];
+        for (int i = 0; i < 6; ++i) g[i] = s_g[k][i];
         float u[6] = {sg[k] * h * (float)S.lin_vel[0], sg[k] * h * (float)S.lin_vel[1], sg[k] * h * (float)S.lin_vel[2],
                       sg[k] * h * (float)S.ang_vel[0], sg[k] * h * (float)S.ang_vel[1], sg[k] * h * (float)S.ang_vel[2]};
+        float gp[6] = {0, 0, 0, 0, 0, 0}, gv[6] = {0, 0, 0, 0, 0, 0};
         M3 RE;
         float tE[3];
         se3_exp(u, RE, tE);
-        adjoint_t_acc(RE, tE, g, gpose);
-        jl_t_acc(u, g, sg[k] * h, gvel);
+        adjoint_t_acc(RE, tE, g, gp);
+        jl_t_acc(u, g, sg[k] * h, gv);
+        for (int i = 0; i < 6; ++i) { s_acc[k][i] = gp[i]; s_acc[k][6 + i] = gv[i]; }
     }
-    // 12-vector in the reference's group order: theta, rho, w, v
-    float grad[12];
-    for (int i = 0; i < 3; ++i) {
-        grad[i] = gpose[3 + i];
-        grad[3 + i] = gpose[i];
-        grad[6 + i] = gvel[3 + i];
-        grad[9 + i] = gvel[i];
-    }
-    for (int i = 0; i < 12; ++i) S.grad[i] = (double)grad[i];
-    for (int p = 0; p < num_pairs; ++p)
-        if (pairs[p].pose == pi) S.loss = loss ? loss[p] : ws.loss_scal[4 * p + 3];
-    bool finite = true;
-    for (int i = 0; i < 12; ++i) finite &= isfinite(grad[i]);
-    if (!finite) {
-        atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
-        return;
-    }
-    // stage control: the velocity learning-rate ramp of the fine stage
-    // (utils/tracker.py:188-202): k = optim_iter - start_vel_opt_iter,
-    // fraction = k / (max_optim_iter / 2) for 1 <= k <= max_optim_iter / 2, else 1;
-    // theta, rho use lr * fraction and w, v use lr * (1 - fraction).
-    if (S.control) {
-        if (S.opt_vel) {
-            const double fnum = 0.5 * (double)S.max_iter;
-            const int k = S.level_iter - S.start_vel;
-            const double frac = (k >= 1 && (double)k <= fnum) ? (double)k / fnum : 1.0;
-            S.lr_scale[0] = S.lr_scale[1] = frac;
-            S.lr_scale[2] = S.lr_scale[3] = 1.0 - frac;
-        } else {
-            S.lr_scale[0] = S.lr_scale[1] = S.lr_scale[2] = S.lr_scale[3] = 1.0;
+    __syncwarp();
+    if (lane == 0) {
+        float gpose[6], gvel[6];
+        for (int i = 0; i < 6; ++i) {
+            gpose[i] = s_acc[0][i] + s_acc[1][i];
+            gvel[i] = s_acc[0][6 + i] + s_acc[1][6 + i];
         }
-    }
-    // Adam with torch's update rule; the parameter is 0 before every step (the deltas are
-    // reset after each update), so the new delta is the step itself
-    float delta[12];
-    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    for (int gi = 0; gi < 4; ++gi) {
-        bool active = gi < 2 || S.opt_vel;
-        for (int k = 0; k < 3; ++k) delta[3 * gi + k] = 0.0f;
-        if (!active) continue;
-        S.step[gi] += 1;
-        float bc1 = 1.0f - powf(b1, (float)S.step[gi]);
-        float bc2 = 1.0f - powf(b2, (float)S.step[gi]);
-        float lr = (float)(S.lr[gi] * S.lr_scale[gi]);
-        for (int k = 0; k < 3; ++k) {
-            int i = 3 * gi + k;
-            float m = b1 * (float)S.m[i] + (1.0f - b1) * grad[i];
-            float v = b2 * (float)S.v[i] + (1.0f - b2) * grad[i] * grad[i];
-            S.m[i] = m;
-            S.v[i] = v;
-            float denom = sqrtf(v) / sqrtf(bc2) + eps;
-            delta[i] = -(lr / bc1) * m / denom;
+        // 12-vector in the reference's group order: theta, rho, w, v
+        float grad[12];
+        for (int i = 0; i < 3; ++i) {
+            grad[i] = gpose[3 + i];
+            grad[3 + i] = gpose[i];
+            grad[6 + i] = gvel[3 + i];
+            grad[9 + i] = gvel[i];
         }
-    }
-    // update_vwRT: velocity first, then the pose
-    if (S.opt_vel)
-        for (int k = 0; k < 3; ++k) { S.ang_vel[k] += delta[6 + k]; S.lin_vel[k] += delta[9 + k]; }
-    float xi[6] = {delta[3], delta[4], delta[5], delta[0], delta[1], delta[2]};
-    M3 Rd;
-    float td[3];
-    se3_exp(xi, Rd, td);
-    double Rn[9], tn[3];
-    for (int i = 0; i < 3; ++i) {
-        for (int j = 0; j < 3; ++j)
-            Rn[3 * i + j] = (double)Rd.a[3 * i] * S.R[j] + (double)Rd.a[3 * i + 1] * S.R[3 + j] +
-                            (double)Rd.a[3 * i + 2] * S.R[6 + j];
-        tn[i] = (double)Rd.a[3 * i] * S.t[0] + (double)Rd.a[3 * i + 1] * S.t[1] + (double)Rd.a[3 * i + 2] * S.t[2] +
-                (double)td[i];
-    }
-    for (int i = 0; i < 9; ++i) S.R[i] = Rn[i];
-    for (int i = 0; i < 3; ++i) S.t[i] = tn[i];
-    S.iter += 1;
-    if (S.control) {
-        // losses.append(loss); converged = mean |diff(last 11 losses)| < threshold
-        // (utils/tracker.py:65-76, 213-217); stage switch / level end (:224-240)
-        S.hist[S.hist_n % 11] = S.loss;
-        S.hist_n += 1;
-        bool converged = false;
-        if (S.hist_n > 10) {
-            double acc = 0.0;
-            for (int q = 0; q < 10; ++q) {
-                const double a = S.hist[(S.hist_n - 11 + q) % 11], b = S.hist[(S.hist_n - 10 + q) % 11];
-                acc += fabs(b - a);
-            }
-            converged = acc / 10.0 < S.conv_thr;
+        bool finite = true;
+        for (int i = 0; i < 12; ++i) {
+            S.grad[i] = (double)grad[i];
+            s_grad[i] = grad[i];
+            finite &= isfinite(grad[i]);
         }
-        if (converged) {
-            if (!S.opt_vel) {
-                S.opt_vel = 1;
-                S.start_vel = S.level_iter;
-                for (int p = 0; p < num_pairs; ++p)
-                    if (pairs[p].pose == pi) pairs[p].unsigned_mode = 0;
+        for (int p = 0; p < num_pairs; ++p)
+            if (pairs[p].pose == pi) S.loss = loss ? loss[p] : ws.loss_scal[4 * p + 3];
+        s_ok = finite;
+        if (!finite) atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
+        // stage control: the velocity learning-rate ramp of the fine stage
+        // (utils/tracker.py:188-202): k = optim_iter - start_vel_opt_iter,
+        // fraction = k / (max_optim_iter / 2) for 1 <= k <= max_optim_iter / 2, else 1;
+        // theta, rho use lr * fraction and w, v use lr * (1 - fraction).
+        if (finite && S.control) {
+            if (S.opt_vel) {
+                const double fnum = 0.5 * (double)S.max_iter;
+                const int k = S.level_iter - S.start_vel;
+                const double frac = (k >= 1 && (double)k <= fnum) ? (double)k / fnum : 1.0;
+                S.lr_scale[0] = S.lr_scale[1] = frac;
+                S.lr_scale[2] = S.lr_scale[3] = 1.0 - frac;
             } else {
-                S.frozen = 1;
+                S.lr_scale[0] = S.lr_scale[1] = S.lr_scale[2] = S.lr_scale[3] = 1.0;
             }
         }
-        if (!S.frozen) {
-            if (!S.opt_vel ? (S.level_iter >= S.max_iter) : (S.level_iter >= S.start_vel + S.max_iter)) S.frozen = 1;
+    }
+    __syncwarp();
+    if (s_ok) {
+        // Adam with torch's update rule, one parameter group per lane; the parameter is 0
+        // before every step (the deltas are reset after each update), so the new delta is
+        // the step itself
+        if (lane < 4) {
+            const int gi = lane;
+            const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+            const bool active = gi < 2 || S.opt_vel;
+            for (int k = 0; k < 3; ++k) s_delta[3 * gi + k] = 0.0f;
+            if (active) {
+                S.step[gi] += 1;
+                const float bc1 = 1.0f - powf(b1, (float)S.step[gi]);
+                const float bc2 = 1.0f - powf(b2, (float)S.step[gi]);
+                const float lr = (float)(S.lr[gi] * S.lr_scale[gi]);
+                for (int k = 0; k < 3; ++k) {
+                    const int i = 3 * gi + k;
+                    const float gr = s_grad[i];
+                    const float m = b1 * (float)S.m[i] + (1.0f - b1) * gr;
+                    const float v = b2 * (float)S.v[i] + (1.0f - b2) * gr * gr;
+                    S.m[i] = m;
+                    S.v[i] = v;
+                    const float denom = sqrtf(v) / sqrtf(bc2) + eps;
+                    s_delta[i] = -(lr / bc1) * m / denom;
+                }
+            }
         }
-        S.level_iter += 1;
+        __syncwarp();
+        if (lane == 0) {
+            // update_vwRT: velocity first, then the pose
+            if (S.opt_vel)
+                for (int k = 0; k < 3; ++k) { S.ang_vel[k] += s_delta[6 + k]; S.lin_vel[k] += s_delta[9 + k]; }
+            float xi[6] = {s_delta[3], s_delta[4], s_delta[5], s_delta[0], s_delta[1], s_delta[2]};
+            M3 Rd;
+            float td[3];
+            se3_exp(xi, Rd, td);
+            double Rn[9], tn[3];
+            for (int i = 0; i < 3; ++i) {
+                for (int j = 0; j < 3; ++j)
+                    Rn[3 * i + j] = (double)Rd.a[3 * i] * S.R[j] + (double)Rd.a[3 * i + 1] * S.R[3 + j] +
+                                    (double)Rd.a[3 * i + 2] * S.R[6 + j];
+                tn[i] = (double)Rd.a[3 * i] * S.t[0] + (double)Rd.a[3 * i + 1] * S.t[1] +
+                        (double)Rd.a[3 * i + 2] * S.t[2] + (double)td[i];
+            }
+            for (int i = 0; i < 9; ++i) S.R[i] = Rn[i];
+            for (int i = 0; i < 3; ++i) S.t[i] = tn[i];
+            S.iter += 1;
+            if (S.control) {
+                // losses.append(loss); converged = mean |diff(last 11 losses)| < threshold
+                // (utils/tracker.py:65-76, 213-217); stage switch / level end (:224-240)
+                S.hist[S.hist_n % 11] = S.loss;
+                S.hist_n += 1;
+                bool converged = false;
+                if (S.hist_n > 10) {
+                    double acc = 0.0;
+                    for (int q = 0; q < 10; ++q) {
+                        const double a = S.hist[(S.hist_n - 11 + q) % 11], b = S.hist[(S.hist_n - 10 + q) % 11];
+                        acc += fabs(b - a);
+                    }
+                    converged = acc / 10.0 < S.conv_thr;
+                }
+                if (converged) {
+                    if (!S.opt_vel) {
+                        S.opt_vel = 1;
+                        S.start_vel = S.level_iter;
+                        for (int p = 0; p < num_pairs; ++p)
+                            if (pairs[p].pose == pi) pairs[p].unsigned_mode = 0;
+                    } else {
+                        S.frozen = 1;
+                    }
+                }
+                if (!S.frozen) {
+                    if (!S.opt_vel ? (S.level_iter >= S.max_iter) : (S.level_iter >= S.start_vel + S.max_iter))
+                        S.frozen = 1;
+                }
+                S.level_iter += 1;
+            }
+        }
+        __syncwarp();
+        // rewrite the pair's view entries for the next iteration (lane k: view k)
+        if (lane < 2) {
+            double Rs[9], ts[3];
+            M3 RE;
+            float tE[3];
+            pair_pose(S, sg[lane], Rs, ts, RE, tE);
+            write_view_pose(views + vids[lane], Rs, ts);
+        }
     }
-    // rewrite the pair's view entries for the next iteration
-    for (int k = 0; k < 2; ++k) {
-        double Rs[9], ts[3];
-        M3 RE;
-        float tE[3];
-        pair_pose(S, sg[k], Rs, ts, RE, tE);
-        write_view_pose(views + vids[k], Rs, ts);
-    }
+    __syncwarp();
+    for (int i = lane; i < WORDS; i += 32) ((uint32_t *)(poses + pi))[i] = ((const uint32_t *)&S)[i];
 }
 
 // Initialise the two view entries of every pose from its current state.
@@ -381,8 +454,8 @@ __global__ void k_view_from_settings(const float *vm_t, const float *pr_t, const
 int gs_launch_track_finalize(const gsevt_frame *f, const Workspace &ws, gsevt_pose_state *poses, int num_poses,
                              const double *loss, cudaStream_t s)
 {
-    k_track_finalize<<<(num_poses + 63) / 64, 64, 0, s>>>((gsevt_view *)f->views, poses, num_poses, ws, loss,
-                                                          (gsevt_pair *)f->pairs, f->L.num_pairs);
+    k_track_finalize<<<num_poses, GS_BLOCK, 0, s>>>((gsevt_view *)f->views, f->maps, poses, num_poses, ws, loss,
+                                                    (gsevt_pair *)f->pairs, f->L.num_pairs);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

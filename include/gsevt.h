@@ -17,8 +17,9 @@
  *     wait that ran out) are recorded in the frame's status words and read back with
  *     gsevt_read_status.
  *   - No entry point allocates device memory: scratch lives in the caller-provided
- *     workspace sized by gsevt_workspace_bytes.
- *   - Re-entrant per stream; no global mutable state.
+ *     workspace sized by gsevt_workspace_bytes (gsevt_events_accumulate_noalloc uses a
+ *     fixed library-owned buffer instead; see its declaration).
+ *   - Re-entrant per stream; no global mutable state other than that buffer.
  */
 #ifndef GSEVT_H
 #define GSEVT_H
@@ -163,9 +164,10 @@ void gsevt_abi_sizes(int32_t *out7);
  * tools), in this order: status, bin, recA, recB, recC, gradA, gradB, gradC, vis_sums,
  * vis_offs, dkeys0, dkeys1, dvals0, dvals1, tsums, toffs, keys0, keys1, vals0, vals1,
  * sort_hist, sort_counter, sort_lookback, ranges, loss_part, loss_scal, loss_done,
- * xi_part, xi (29 entries; absent regions are reported as UINT64_MAX).  keys are 32-bit
- * global tile ids, vals 32-bit (view, Gaussian) slots.  Touches no GPU state. */
-void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out29);
+ * xi_part, xi, csums, coffs, soffs, sranges (33 entries; absent regions are reported
+ * as UINT64_MAX).  keys are 32-bit global tile ids, vals 32-bit (view, Gaussian)
+ * slots.  Touches no GPU state. */
+void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out33);
 
 /* ---- map packing ----
  * Replaces the per-call activation + torch.cat of get_features

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 import torch
 
+from gsevt import _lib
 from gsevt import pose as gpose
 from gsevt import synthetic
 from gsevt.batched import BatchedTracker, Problem
@@ -71,6 +72,63 @@ def test_batched_problems_match_single_launches():
         assert np.linalg.norm(g1 - g2) <= 1e-5 * np.linalg.norm(g1), (pi, g1, g2)
         np.testing.assert_allclose(ss["R"][0], st["R"][slot], atol=1e-7)
         np.testing.assert_allclose(ss["t"][0], st["t"][slot], atol=1e-7)
+
+
+def _ws_region(frame, name, dtype, count):
+    off = _lib.workspace_offsets(frame.L)[name]
+    nbytes = count * torch.empty((), dtype=dtype).element_size()
+    return frame.workspace[off:off + nbytes].view(dtype)
+
+
+@pytest.mark.parametrize("sizes", [((320, 240, 300.0), (256, 192, 220.0)), ((640, 480, 600.0), (1280, 720, 900.0))])
+def test_super_tile_lists_match_tile_sort(sizes):
+    """The batched step bins through 4x4-tile super-tiles; its per-tile lists, ranges and
+    images equal the full stable tile sort of gsevt_bin_and_sort on the same views."""
+    (w0, h0, f0), (w1, h1, f1) = sizes
+    s0, pk0, sig0, _, _ = _scenario(20000, w0, h0, f0, 5, 30000)
+    s1, pk1, sig1, _, _ = _scenario(15000, w1, h1, f1, 6, 30000)
+    maps = [{"packed": pk0, "n": 20000}, {"packed": pk1, "n": 15000}]
+    def prob(sc, mi, E, seed):
+        R, t = synthetic.perturb(sc.gt_R, sc.gt_t, np.random.default_rng(seed), 0.05, 3.0)
+        c = sc.camera
+        return Problem(mi, R, t, sc.init_lin, sc.init_ang, sc.delta_tau, c.width, c.height, c.fx, c.fy,
+                       E.reshape(-1), opt_vel=True)
+    probs = [prob(s0, 0, sig0[0], 20), prob(s1, 1, sig1[0], 21), prob(s0, 0, sig0[0], 22)]
+    bt = BatchedTracker(maps, probs, device=DEV)
+    fr = bt.frame
+    L = fr.L
+    views0 = fr.view_table.clone()
+    bt.step()
+    torch.cuda.synchronize()
+    st, _ = fr.status()
+    assert st == 0, st
+    # the super-tile sort ends in buffer (passes & 1); the fine lists are in the other one
+    bound = L.total_tiles // 4 + L.num_views + 1
+    bits = max(1, int(bound - 1).bit_length())
+    fine_buf = (((bits + 7) // 8) & 1) ^ 1
+    T = L.total_tiles
+    img_c = fr.image.clone()
+    rng_c = _ws_region(fr, "ranges", torch.int32, 2 * T).view(T, 2).clone().cpu().numpy()
+    vals_c = _ws_region(fr, "vals%d" % fine_buf, torch.int32, L.key_capacity).clone().cpu().numpy()
+    # the full tile sort on the same view table
+    fr.view_table.copy_(views0)
+    fr.preprocess()
+    fr.bin_and_sort()
+    fr.blend()
+    torch.cuda.synchronize()
+    st, K = fr.status()
+    assert st == 0, st
+    tile_buf = ((L.sort_bits - 32 + 7) // 8) & 1
+    rng_f = _ws_region(fr, "ranges", torch.int32, 2 * T).view(T, 2).cpu().numpy()
+    vals_f = _ws_region(fr, "vals%d" % tile_buf, torch.int32, L.key_capacity).cpu().numpy()
+    assert (rng_f[:, 1] - rng_f[:, 0]).sum() == K
+    np.testing.assert_array_equal(rng_c[:, 1] - rng_c[:, 0], rng_f[:, 1] - rng_f[:, 0])
+    for t in range(T):
+        a, b = rng_c[t]
+        c, d = rng_f[t]
+        if b > a:
+            assert np.array_equal(vals_c[a:b], vals_f[c:d]), t
+    assert torch.equal(img_c, fr.image)
 
 
 def test_batched_converges_like_plain():
