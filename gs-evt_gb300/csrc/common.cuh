@@ -81,7 +81,7 @@ struct Workspace {
     double *loss_part;    // [loss_blocks][4]
     double *loss_scal;    // [num_pairs][4] {s, cross, e2, L}
     uint32_t *loss_done;  // [num_pairs]
-    double *xi_part;      // [num_scan_blocks][6]
+    double *xi_part;      // [num_scan_blocks][6] float pairs (hi, lo) of the block's twist sums
     double *xi;           // [num_views][6]
     // super-tile binning (batched tracker): 4x4-tile super-tiles, numbered per view
     uint32_t *csums;      // [sorted blocks] super-tiles touched per block of depth-sorted slots

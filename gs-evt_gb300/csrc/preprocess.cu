@@ -539,7 +539,10 @@ __global__ void __launch_bounds__(GS_BLOCK, MAPGRAD ? 1 : 2) k_preprocess_bwd(Bw
         if (threadIdx.x < 6) {
             double s = 0.0;
             for (int w = 0; w < GS_BLOCK / 32; ++w) s += wpart[w][threadIdx.x];
-            p.ws.xi_part[(size_t)(V.sb_offset + gb) * 6 + threadIdx.x] = s;
+            // stored as an unevaluated float pair hi + lo (48 significant bits), which
+            // the per-view sums can add with FP32 error-free transformations
+            const float hi = (float)s, lo = (float)(s - (double)hi);
+            ((float2 *)p.ws.xi_part)[(size_t)(V.sb_offset + gb) * 6 + threadIdx.x] = make_float2(hi, lo);
         }
     }
     if (MAPGRAD && valid && p.grads) {
@@ -602,7 +605,10 @@ __global__ void k_xi_reduce(const gsevt_view *views, const gsevt_map *maps, Work
     __shared__ double part[GS_BLOCK / 32][6];
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int i = threadIdx.x; i < nb; i += blockDim.x)
-        for (int k = 0; k < 6; ++k) acc[k] += ws.xi_part[(size_t)(V.sb_offset + i) * 6 + k];
+        for (int k = 0; k < 6; ++k) {
+            const float2 e = ((const float2 *)ws.xi_part)[(size_t)(V.sb_offset + i) * 6 + k];
+            acc[k] += (double)e.x + (double)e.y;
+        }
     for (int k = 0; k < 6; ++k) {
         double s = warp_sum_d(acc[k]);
         if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5][k] = s;

@@ -1,9 +1,10 @@
 // Pose algebra on the device: the exact chain from per-view twist gradients to the
 // reference's 12 optimised deltas, the Adam step and the pose / velocity update of the
 // batched tracker, and the drop-in helpers (view entry from settings tensors, chain of
-// one view's gradient).  The per-view gradient sums arrive in FP64 (the one FP64
-// reduction of the path); the chain, Adam and exponential maps run in FP32, as the
-// reference's own pose parameters do, and the pose itself is stored and composed in FP64.
+// one view's gradient).  The per-view gradient sums are formed from per-block float
+// pairs with error-free FP32 arithmetic (about 48 significant bits); the chain, Adam and
+// exponential maps run in FP32, as the reference's own pose parameters do, and the pose
+// itself is stored and composed in FP64.
 //
 // Pose conventions follow the reference:
 //   SE3_exp([rho, theta]) with the SO(3) left Jacobian V (utils/pose.py:26-91);
@@ -150,42 +151,60 @@ __device__ inline void jl_t_acc(const float *xi, const float *g, float sc, float
     for (int i = 0; i < 3; ++i) { out6[i] += sc * a[i]; out6[3 + i] += sc * (b[i] + c[i]); }
 }
 
-// rendered pose of role s (-1 last, +1 next): E_s T, with E_s = SE3_exp(s h [v, w]);
-// the product with the stored FP64 pose is formed in FP64.
-__device__ inline void pair_pose(const gsevt_pose_state &S, float sgn, double *Rs, double *ts, M3 &RE, float *tE)
+// Unevaluated float pair hi + lo, added with Knuth's TwoSum (exact error of each FP32
+// addition; every operation rounds separately because the library is built with
+// -fmad=false).
+struct FF {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ void add(float xh, float xl)
+    {
+        const float t = hi + xh, z = t - hi;
+        const float e = (hi - (t - z)) + (xh - z);
+        hi = t;
+        lo = lo + (e + xl);
+        const float u = hi + lo;  // renormalise
+        lo = lo - (u - hi);
+        hi = u;
+    }
+};
+
+// rendered pose of role s (-1 last, +1 next): E_s T, with E_s = SE3_exp(s h [v, w]); the
+// view entries are FP32, so the product is formed in FP32 from the rounded pose.
+__device__ inline void pair_pose(const gsevt_pose_state &S, float sgn, float *Rs, float *ts, M3 &RE, float *tE)
 {
     float h = (float)(S.delta_tau * 0.5);
     float u[6] = {sgn * h * (float)S.lin_vel[0], sgn * h * (float)S.lin_vel[1], sgn * h * (float)S.lin_vel[2],
                   sgn * h * (float)S.ang_vel[0], sgn * h * (float)S.ang_vel[1], sgn * h * (float)S.ang_vel[2]};
     se3_exp(u, RE, tE);
+    float R[9], t[3];
+    for (int i = 0; i < 9; ++i) R[i] = (float)S.R[i];
+    for (int i = 0; i < 3; ++i) t[i] = (float)S.t[i];
     for (int i = 0; i < 3; ++i) {
         for (int j = 0; j < 3; ++j)
-            Rs[3 * i + j] = (double)RE.a[3 * i] * S.R[j] + (double)RE.a[3 * i + 1] * S.R[3 + j] +
-                            (double)RE.a[3 * i + 2] * S.R[6 + j];
-        ts[i] = (double)RE.a[3 * i] * S.t[0] + (double)RE.a[3 * i + 1] * S.t[1] + (double)RE.a[3 * i + 2] * S.t[2] +
-                (double)tE[i];
+            Rs[3 * i + j] = RE.a[3 * i] * R[j] + RE.a[3 * i + 1] * R[3 + j] + RE.a[3 * i + 2] * R[6 + j];
+        ts[i] = ((RE.a[3 * i] * t[0] + RE.a[3 * i + 1] * t[1]) + RE.a[3 * i + 2] * t[2]) + tE[i];
     }
 }
 
-__device__ inline void write_view_pose(gsevt_view *V, const double *R, const double *t)
+__device__ inline void write_view_pose(gsevt_view *V, const float *R, const float *t)
 {
-    for (int i = 0; i < 9; ++i) V->R[i] = (float)R[i];
-    for (int i = 0; i < 3; ++i) V->t[i] = (float)t[i];
-    for (int i = 0; i < 3; ++i)
-        V->campos[i] = (float)(-(R[i] * t[0] + R[3 + i] * t[1] + R[6 + i] * t[2]));
+    for (int i = 0; i < 9; ++i) V->R[i] = R[i];
+    for (int i = 0; i < 3; ++i) V->t[i] = t[i];
+    for (int i = 0; i < 3; ++i) V->campos[i] = -(R[i] * t[0] + R[3 + i] * t[1] + R[6 + i] * t[2]);
 }
 
 // One block per pose.  The block sums the per-scan-block twist partials of the pose's two
-// views (FP64; thread i adds partials i, i + 256, ... in order, four loads in flight, then
-// warp and block sums in a fixed order - the order of k_xi_reduce), with the pose state
-// staged in shared memory.  Warp 0 then runs the serial part with its lanes sharing the
+// views as float pairs with error-free FP32 transformations (about 48 significant bits;
+// GB300's FP64 rate would make plain double sums the slowest part of the kernel): thread
+// i adds partials i, i + 256, ... in order, four loads in flight, then warp and block
+// combinations in a fixed order.  The pose state is staged in shared memory.  Warp 0 then runs the serial part with its lanes sharing the
 // independent pieces: the two views' chain terms (lanes 0, 1), the four Adam groups
 // (lanes 0-3), the pose update (lane 0) and the two view rewrites (lanes 0, 1).
 __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, const gsevt_map *maps,
                                                              gsevt_pose_state *poses, int num_poses, Workspace ws,
                                                              const double *loss, gsevt_pair *pairs, int num_pairs)
 {
-    __shared__ double part[2][GS_BLOCK / 32][6];
+    __shared__ float2 part[2][GS_BLOCK / 32][6];
     __shared__ gsevt_pose_state S;
     __shared__ float s_g[2][6], s_acc[2][12], s_grad[12], s_delta[12];
     __shared__ int s_ok;
@@ -200,33 +219,43 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
     for (int k = 0; k < 2; ++k) {
         const gsevt_view &V = views[vids[k]];
         const int nb = (maps[V.map].n + GS_BLOCK - 1) / GS_BLOCK;
-        const double *xp = ws.xi_part + (size_t)V.sb_offset * 6;
-        double acc[6] = {0, 0, 0, 0, 0, 0};
+        const float2 *xp = (const float2 *)ws.xi_part + (size_t)V.sb_offset * 6;
+        FF acc[6];
         for (int i0 = threadIdx.x; i0 < nb; i0 += 4 * GS_BLOCK) {
-            double x[4][6];
+            float2 x[4][6];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int i = i0 + j * GS_BLOCK;
 #pragma unroll
-                for (int q = 0; q < 6; ++q) x[j][q] = i < nb ? xp[(size_t)i * 6 + q] : 0.0;
+                for (int q = 0; q < 6; ++q) x[j][q] = i < nb ? xp[(size_t)i * 6 + q] : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
             for (int j = 0; j < 4; ++j)
 #pragma unroll
-                for (int q = 0; q < 6; ++q) acc[q] += x[j][q];
+                for (int q = 0; q < 6; ++q) acc[q].add(x[j][q].x, x[j][q].y);
         }
         for (int q = 0; q < 6; ++q) {
-            const double sm = warp_sum_d(acc[q]);
-            if ((threadIdx.x & 31) == 0) part[k][threadIdx.x >> 5][q] = sm;
+            FF sm = acc[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float hi = __shfl_xor_sync(0xffffffffu, sm.hi, o), lo = __shfl_xor_sync(0xffffffffu, sm.lo, o);
+                // combine in lane order so that both partners form the same sum
+                FF a = ((threadIdx.x & o) == 0) ? sm : FF{hi, lo};
+                const FF b2 = ((threadIdx.x & o) == 0) ? FF{hi, lo} : sm;
+                a.add(b2.hi, b2.lo);
+                sm = a;
+            }
+            if ((threadIdx.x & 31) == 0) part[k][threadIdx.x >> 5][q] = make_float2(sm.hi, sm.lo);
         }
     }
     __syncthreads();
     if (threadIdx.x < 12) {
         const int k = threadIdx.x / 6, q = threadIdx.x % 6;
-        double sm = 0;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) sm += part[k][w][q];
-        ws.xi[6 * vids[k] + q] = sm;
-        s_g[k][q] = (float)sm;
+        FF sm;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) sm.add(part[k][w][q].x, part[k][w][q].y);
+        const double v = (double)sm.hi + (double)sm.lo;
+        ws.xi[6 * vids[k] + q] = v;
+        s_g[k][q] = (float)v;
     }
     __syncthreads();
     if (threadIdx.x >= 32) return;
@@ -370,7 +399,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
         __syncwarp();
         // rewrite the pair's view entries for the next iteration (lane k: view k)
         if (lane < 2) {
-            double Rs[9], ts[3];
+            float Rs[9], ts[3];
             M3 RE;
             float tE[3];
             pair_pose(S, sg[lane], Rs, ts, RE, tE);
@@ -390,7 +419,7 @@ __global__ void k_track_views(gsevt_view *views, const gsevt_pose_state *poses, 
     const int vids[2] = {S.last_view, S.next_view};
     const float sg[2] = {-1.0f, 1.0f};
     for (int k = 0; k < 2; ++k) {
-        double Rs[9], ts[3];
+        float Rs[9], ts[3];
         M3 RE;
         float tE[3];
         pair_pose(S, sg[k], Rs, ts, RE, tE);
