@@ -547,11 +547,13 @@ def main():
             traffic = json.load(open(tpath)).get(args.workload, {}).get(top)
         except Exception:
             traffic = None
-    # kernels per iteration: preprocess, 2 scans, compaction, depth sort (hist, epoch, 4 passes),
-    # sorted sums, duplication, tile sort (hist, epoch, passes), ranges, blend fwd, loss,
-    # blend bwd, preprocess bwd, twist reduction, finalize
-    tile_passes = (bt.frame.L.sort_bits - 32 + 7) // 8
-    launches_per_iter = 21 + tile_passes
+    # kernels per iteration of the batched step: preprocess, scan, compaction, depth sort
+    # (histogram, 4 passes), sorted sums, paired scan, coarse duplication, super-tile sort
+    # (histogram, passes), super-tile ranges, tile filter, blend fwd, loss, blend bwd,
+    # preprocess bwd, finalize
+    L = bt.frame.L
+    super_bits = max(1, int(L.total_tiles // 4 + L.num_views).bit_length())
+    launches_per_iter = 18 + (super_bits + 7) // 8
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
