@@ -341,10 +341,10 @@ __device__ __forceinline__ uint32_t cover_mask(uint32_t lo, uint32_t hi, int X, 
     return m;
 }
 
-// One block per super-tile (32 warps); warp w takes the w-th contiguous 32nd of the
-// super-tile's depth-ordered coarse list, four groups of 32 entries at a time (their
-// loads in flight together).  Pass 1 counts, per warp and tile, the entries whose
-// rectangle covers the tile (one ballot per tile per group); the block then claims a
+// One block per super-tile (16 warps, two blocks per SM); warp w takes the w-th
+// contiguous sixteenth of the super-tile's depth-ordered coarse list, four groups of 32
+// entries at a time (their loads in flight together).  Pass 1 counts, per warp and
+// tile, the entries whose rectangle covers the tile; the block then claims a
 // contiguous region of the fine list with one atomic add and lays its 16 tile lists out
 // in it; pass 2 rescans the same entries and writes each one into the lists of the tiles
 // it covers, at (tile start + earlier warps' count + running count + rank in the ballot).
@@ -353,7 +353,7 @@ __device__ __forceinline__ uint32_t cover_mask(uint32_t lo, uint32_t hi, int X, 
 // tile of the super-tile; their placement in the fine list follows the order in which
 // blocks claim regions, which does not affect any tile's content.
 #define FILTER_TILES (GS_SUPER * GS_SUPER)
-#define FILTER_WARPS 32
+#define FILTER_WARPS 16
 #define FILTER_ILP 4
 __device__ __forceinline__ void filter_load(const uint32_t *cvals, const int4 *bin, uint32_t g, uint32_t b1,
                                             int lane, int X, int Y, uint32_t (&vg)[FILTER_ILP],
@@ -397,18 +397,21 @@ __global__ void __launch_bounds__(FILTER_WARPS * 32) k_filter_tiles(const gsevt_
     const uint32_t b0 = sr.x + min(len, (uint32_t)w * seg), b1 = sr.x + min(len, (uint32_t)(w + 1) * seg);
     const uint32_t lt = (1u << lane) - 1u;
 
-    // pass 1: per-tile counts of this warp's entries (lane t holds tile t's count)
+    // pass 1: per-tile counts of this warp's entries (lane t holds tile t's count).  Each
+    // lane spreads its 16-bit mask over four words, one byte per tile (x * 0x00204081
+    // moves bit i of a nibble to bit 8 i), so four warp-wide integer sums count all 16
+    // tiles at once (a group of 32 entries contributes at most 32 per byte).
     uint32_t cnt = 0;
     for (uint32_t g = b0; g < b1; g += 32 * FILTER_ILP) {
         uint32_t vg[FILTER_ILP], m[FILTER_ILP];
         filter_load(cvals, ws.bin, g, b1, lane, X, Y, vg, m);
 #pragma unroll
         for (int k = 0; k < FILTER_ILP; ++k) {
+            uint32_t packed[4];
 #pragma unroll
-            for (int t = 0; t < FILTER_TILES; ++t) {
-                const uint32_t bal = __ballot_sync(0xffffffffu, (m[k] >> t) & 1u);
-                if (lane == t) cnt += __popc(bal);
-            }
+            for (int r = 0; r < 4; ++r)
+                packed[r] = __reduce_add_sync(0xffffffffu, (((m[k] >> (4 * r)) & 0xfu) * 0x00204081u) & 0x01010101u);
+            cnt += (packed[(lane >> 2) & 3] >> (8 * (lane & 3))) & 0xffu;
         }
     }
     if (lane < FILTER_TILES) s_cnt[w][lane] = cnt;

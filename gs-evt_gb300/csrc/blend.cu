@@ -414,7 +414,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                                 if (RGB) { const float4 Cc = cur.C[j]; col[0] = Cc.x; col[1] = Cc.y; col[2] = Cc.z; }
                                 else { col[0] = A.w; col[1] = col[2] = 0.0f; }
                                 const float wgt = alpha * T;
-                                const float inv1m = 1.0f / (1.0f - alpha);
+                                // gradient-only term: the 2-ulp fast reciprocal suffices
+                                const float inv1m = __fdividef(1.0f, 1.0f - alpha);
                                 float dal = 0.0f;
 #pragma unroll
                                 for (int c = 0; c < (RGB ? 3 : 1); ++c) {
