@@ -148,7 +148,10 @@ __device__ __forceinline__ void warp_pixel(int tid, int tx, int ty, int &px, int
     sy1 = (float)(by + 3);
 }
 
-template <bool DEPTH, bool RGB>
+// EXTRAS: the frame wants depth, alpha, contributor counts or n_touched (each still
+// checked at run time); without it only the image and the final transmittance are
+// accumulated (the batched tracker's case).
+template <bool EXTRAS, bool RGB>
 __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams p)
 {
     __shared__ Batch<RGB> sb[2];
@@ -185,7 +188,7 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
             float4 e;
             cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &e);
             cur.ell[threadIdx.x] = e;
-            if (!DEPTH) cur.A[threadIdx.x].z = e.w;  // depth is not needed: keep the threshold in its slot
+            if (!EXTRAS) cur.A[threadIdx.x].z = e.w;  // depth is not needed: keep the threshold in its slot
         }
         __syncthreads();
         bool warp_done = false;
@@ -210,7 +213,7 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
                 const float dx = A.x - pxf, dy = A.y - pyf;
                 const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
                 // power > 0, or below the Gaussian's alpha threshold (fails the alpha test anyway)
-                if (power > 0.0f || power < (DEPTH ? cur.ell[j].w : A.z)) continue;
+                if (power > 0.0f || power < (EXTRAS ? cur.ell[j].w : A.z)) continue;
                 const float alpha = fminf(0.99f, B.w * gs_expf(power));
                 if (alpha < 1.0f / 255.0f) continue;
                 const float test_T = T * (1.0f - alpha);
@@ -223,11 +226,13 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
                 } else {
                     C0 = C0 + (A.w * alpha) * T;
                 }
-                if (DEPTH) D = D + (A.z * alpha) * T;
-                Aacc = Aacc + alpha * T;
-                if (p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
+                if (EXTRAS) {
+                    D = D + (A.z * alpha) * T;
+                    Aacc = Aacc + alpha * T;
+                    if (p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
+                    last = r * GS_BLOCK + j + 1;
+                }
                 T = test_T;
-                last = r * GS_BLOCK + j + 1;
             }
         }
         __syncthreads();  // the next iteration overwrites this buffer
@@ -245,9 +250,11 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
             p.image[pix] = C0 + T * bgg;
         }
         p.final_T[pix] = T;
-        if (p.depth) p.depth[pix] = D;
-        if (p.alpha) p.alpha[pix] = Aacc;
-        if (p.n_contrib) p.n_contrib[pix] = last;
+        if (EXTRAS) {
+            if (p.depth) p.depth[pix] = D;
+            if (p.alpha) p.alpha[pix] = Aacc;
+            if (p.n_contrib) p.n_contrib[pix] = last;
+        }
     }
 }
 
@@ -506,11 +513,12 @@ int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     BlendParams p = make_params(f, ws, vals);
     if (f->n_touched) cudaMemsetAsync(f->n_touched, 0, (size_t)f->L.num_vg * 4, s);
     const int n = f->L.total_tiles;
+    const bool extras = f->depth || f->alpha || f->n_contrib || f->n_touched;
     if (p.rgb) {
-        if (f->depth) k_blend_fwd<true, true><<<n, GS_BLOCK, 0, s>>>(p);
+        if (extras) k_blend_fwd<true, true><<<n, GS_BLOCK, 0, s>>>(p);
         else k_blend_fwd<false, true><<<n, GS_BLOCK, 0, s>>>(p);
     } else {
-        if (f->depth) k_blend_fwd<true, false><<<n, GS_BLOCK, 0, s>>>(p);
+        if (extras) k_blend_fwd<true, false><<<n, GS_BLOCK, 0, s>>>(p);
         else k_blend_fwd<false, false><<<n, GS_BLOCK, 0, s>>>(p);
     }
     GS_CUDA_CHECK();

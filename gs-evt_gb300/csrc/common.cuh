@@ -196,6 +196,44 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
+// Unevaluated float pair hi + lo, added with Knuth's TwoSum (exact error of each FP32
+// addition; every operation rounds separately because the library is built with
+// -fmad=false): about 48 significant bits at FP32 cost.
+struct FP2 {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ void add(float xh, float xl)
+    {
+        const float t = hi + xh, z = t - hi;
+        const float e = (hi - (t - z)) + (xh - z);
+        hi = t;
+        lo = lo + (e + xl);
+        const float u = hi + lo;  // renormalise
+        lo = lo - (u - hi);
+        hi = u;
+    }
+    __device__ void add(const FP2 &x) { add(x.hi, x.lo); }
+};
+
+// warp sum of one float per lane as a float pair, combined in lane order (every lane
+// gets the same result)
+__device__ __forceinline__ FP2 warp_sum_fp2(float v)
+{
+    FP2 sm;
+    sm.hi = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float hi = __shfl_xor_sync(0xffffffffu, sm.hi, o), lo = __shfl_xor_sync(0xffffffffu, sm.lo, o);
+        FP2 other;
+        other.hi = hi;
+        other.lo = lo;
+        FP2 a = ((threadIdx.x & o) == 0) ? sm : other;
+        const FP2 b = ((threadIdx.x & o) == 0) ? other : sm;
+        a.add(b);
+        sm = a;
+    }
+    return sm;
+}
+
 __device__ __forceinline__ double warp_sum_d(double v)
 {
 #pragma unroll

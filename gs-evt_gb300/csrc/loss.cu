@@ -5,8 +5,8 @@
 // ~8 forward and ~10 backward torch kernels per iteration.  With s = ||dI||,
 // c = sum(dI E) (signed) or sum(|dI| |E|) (unsigned) and e2 = sum(E^2),
 //   L^2 = 1 - 2 c / s + e2,
-// so one reduction pass gives L (FP32 over each thread's 8 pixels, FP64 from the warp
-// level up); the per-pixel gradient
+// so one reduction pass gives L (FP32 over each thread's 8 pixels, float pairs with
+// error-free additions within a block, FP64 across blocks); the per-pixel gradient
 //   dL/dI_next = -dL/dI_last = (g - n (n.g)) / s,  n.g = (1 - c/s) / L,
 // is formed inside the blend adjoint from (s, c, L) without another pass.
 // Each block reduces a slice of one pair into FP64 partials; the last block of the
@@ -31,7 +31,8 @@ __device__ __forceinline__ int find_pair(const gsevt_pair *pairs, int num_pairs,
 __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, const gsevt_pair *pairs, int num_pairs,
                                                    const float *image, Workspace ws, double *loss_out)
 {
-    __shared__ double part[GS_BLOCK / 32][3];
+    __shared__ FP2 part[GS_BLOCK / 32][3];
+    __shared__ double dpart[GS_BLOCK / 32][3];
     __shared__ bool is_last;
     const int b = blockIdx.x;
     const int pi = find_pair(pairs, num_pairs, b);
@@ -54,7 +55,9 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
             cr = pr.unsigned_mode ? fmaf(fabsf(d), fabsf(e), cr) : fmaf(d, e, cr);
         }
     }
-    double S2 = warp_sum_d((double)s2), CR = warp_sum_d((double)cr), E2 = warp_sum_d((double)e2);
+    // warp and block sums as float pairs (error-free FP32 additions; GB300's FP64 rate
+    // would make double arithmetic the slow part), converted to FP64 once per block
+    FP2 S2 = warp_sum_fp2(s2), CR = warp_sum_fp2(cr), E2 = warp_sum_fp2(e2);
     if ((threadIdx.x & 31) == 0) {
         part[threadIdx.x >> 5][0] = S2;
         part[threadIdx.x >> 5][1] = CR;
@@ -62,9 +65,9 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     }
     __syncthreads();
     if (threadIdx.x < 3) {
-        double t = 0.0;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) t += part[w][threadIdx.x];
-        ws.loss_part[(size_t)b * 4 + threadIdx.x] = t;
+        FP2 t;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) t.add(part[w][threadIdx.x]);
+        ws.loss_part[(size_t)b * 4 + threadIdx.x] = (double)t.hi + (double)t.lo;
     }
     __threadfence();
     __syncthreads();
@@ -90,14 +93,14 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     a2 = warp_sum_d(a2);
     __syncthreads();
     if ((threadIdx.x & 31) == 0) {
-        part[threadIdx.x >> 5][0] = a0;
-        part[threadIdx.x >> 5][1] = a1;
-        part[threadIdx.x >> 5][2] = a2;
+        dpart[threadIdx.x >> 5][0] = a0;
+        dpart[threadIdx.x >> 5][1] = a1;
+        dpart[threadIdx.x >> 5][2] = a2;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         double S2t = 0, CRt = 0, E2t = 0;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) { S2t += part[w][0]; CRt += part[w][1]; E2t += part[w][2]; }
+        for (int w = 0; w < GS_BLOCK / 32; ++w) { S2t += dpart[w][0]; CRt += dpart[w][1]; E2t += dpart[w][2]; }
         double s = sqrt(S2t);
         double L2 = 1.0 - 2.0 * CRt / s + E2t;
         double L = sqrt(L2 > 0.0 ? L2 : 0.0);

@@ -151,22 +151,6 @@ __device__ inline void jl_t_acc(const float *xi, const float *g, float sc, float
     for (int i = 0; i < 3; ++i) { out6[i] += sc * a[i]; out6[3 + i] += sc * (b[i] + c[i]); }
 }
 
-// Unevaluated float pair hi + lo, added with Knuth's TwoSum (exact error of each FP32
-// addition; every operation rounds separately because the library is built with
-// -fmad=false).
-struct FF {
-    float hi = 0.0f, lo = 0.0f;
-    __device__ void add(float xh, float xl)
-    {
-        const float t = hi + xh, z = t - hi;
-        const float e = (hi - (t - z)) + (xh - z);
-        hi = t;
-        lo = lo + (e + xl);
-        const float u = hi + lo;  // renormalise
-        lo = lo - (u - hi);
-        hi = u;
-    }
-};
 
 // rendered pose of role s (-1 last, +1 next): E_s T, with E_s = SE3_exp(s h [v, w]); the
 // view entries are FP32, so the product is formed in FP32 from the rounded pose.
@@ -220,7 +204,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
         const gsevt_view &V = views[vids[k]];
         const int nb = (maps[V.map].n + GS_BLOCK - 1) / GS_BLOCK;
         const float2 *xp = (const float2 *)ws.xi_part + (size_t)V.sb_offset * 6;
-        FF acc[6];
+        FP2 acc[6];
         for (int i0 = threadIdx.x; i0 < nb; i0 += 4 * GS_BLOCK) {
             float2 x[4][6];
 #pragma unroll
@@ -235,13 +219,16 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
                 for (int q = 0; q < 6; ++q) acc[q].add(x[j][q].x, x[j][q].y);
         }
         for (int q = 0; q < 6; ++q) {
-            FF sm = acc[q];
+            FP2 sm = acc[q];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 const float hi = __shfl_xor_sync(0xffffffffu, sm.hi, o), lo = __shfl_xor_sync(0xffffffffu, sm.lo, o);
                 // combine in lane order so that both partners form the same sum
-                FF a = ((threadIdx.x & o) == 0) ? sm : FF{hi, lo};
-                const FF b2 = ((threadIdx.x & o) == 0) ? FF{hi, lo} : sm;
+                FP2 oth;
+                oth.hi = hi;
+                oth.lo = lo;
+                FP2 a = ((threadIdx.x & o) == 0) ? sm : oth;
+                const FP2 b2 = ((threadIdx.x & o) == 0) ? oth : sm;
                 a.add(b2.hi, b2.lo);
                 sm = a;
             }
@@ -251,7 +238,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
     __syncthreads();
     if (threadIdx.x < 12) {
         const int k = threadIdx.x / 6, q = threadIdx.x % 6;
-        FF sm;
+        FP2 sm;
         for (int w = 0; w < GS_BLOCK / 32; ++w) sm.add(part[k][w][q].x, part[k][w][q].y);
         const double v = (double)sm.hi + (double)sm.lo;
         ws.xi[6 * vids[k] + q] = v;
