@@ -5,6 +5,7 @@
 #include "common.cuh"
 
 int gs_launch_preprocess_fwd(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
+int gs_launch_preprocess_bwd_cached(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
 int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gsevt_map_grads *grads_dev,
                              double *xi_out, cudaStream_t s,
                              bool reduce);
@@ -85,7 +86,7 @@ extern "C" void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out)
                                        w.tsums, w.toffs, w.keys[0], w.keys[1], w.vals[0], w.vals[1], w.sort_hist,
                                        w.sort_counter, w.sort_lookback, w.ranges, w.loss_part, w.loss_scal,
                                        w.loss_done, w.xi_part, w.xi, w.csums, w.coffs, w.soffs,
-                                       w.sranges};
+                                       w.sranges, w.fcache};
     for (int i = 0; i < GS_WS_REGIONS; ++i)
         out[i] = ptrs[i] ? (uint64_t)((const char *)ptrs[i] - base) : UINT64_MAX;
 }
@@ -200,6 +201,6 @@ extern "C" int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *
     if ((st = gs_launch_blend_fwd(f, ws, fine, s))) return st;
     if ((st = gs_launch_loss(f, ws, loss_out, s))) return st;
     if ((st = gs_launch_blend_bwd(f, ws, fine, nullptr, nullptr, nullptr, s))) return st;
-    if ((st = gs_launch_preprocess_bwd(f, ws, nullptr, nullptr, s, false))) return st;
+    if ((st = gs_launch_preprocess_bwd_cached(f, ws, s))) return st;
     return gs_launch_track_finalize(f, ws, poses, num_poses, loss_out, s);
 }

@@ -88,10 +88,13 @@ struct Workspace {
     uint32_t *coffs;      // [sorted blocks]
     uint32_t *soffs;      // [num_views + 1] first super-tile of each view; [num_views] = total
     uint2 *sranges;       // [gs_super_bound] [start, end) of every super-tile in the sorted coarse pairs
+    float4 *fcache;       // [num_vg][6] forward intermediates of each visible slot for the
+                          // twist-only adjoint (frames with render pairs; else absent)
     size_t bytes;
 };
 
-#define GS_WS_REGIONS 33
+#define GS_WS_REGIONS 34
+#define GS_FCACHE 6       // float4 words per slot in fcache
 #define GS_SUPER 4   // tiles per super-tile side
 
 __host__ __device__ inline size_t gs_align(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -165,6 +168,7 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     w.coffs = (uint32_t *)take((size_t)gs_sorted_blocks(L) * 4);
     w.soffs = (uint32_t *)take((size_t)(L.num_views + 1) * 4);
     w.sranges = (uint2 *)take((size_t)gs_super_bound(L) * 8);
+    w.fcache = (L.num_pairs > 0 && !rgb) ? (float4 *)take(vg * GS_FCACHE * 16) : nullptr;
     w.bytes = off;
     return w;
 }

@@ -224,6 +224,51 @@ __device__ __forceinline__ void load_attr(const gsevt_map &M, int g, Attr &a)
     }
 }
 
+__device__ __forceinline__ void sh_dir_grad(int deg, const float *w, float x, float y, float z, float *g);
+
+// Forward intermediates of one visible slot that the twist-only adjoint needs, so that it
+// reads 96 bytes per slot instead of the map attributes and the recomputed forward:
+//   c0 {cov2 a, b, c, det}, c1 {T0 S (3), T1 S x}, c2 {T1 S y, z, J00, J02},
+//   c3 {J11, J12, pc x, pc y}, c4 {pc z, pw, hom x, hom y}, c5 {U (3), clamp flags},
+// with S the world covariance, T0, T1 the rows of J W, and U the direction term of the
+// grey colour: for a grey gradient g, the SH view-direction gradient of the slot is
+// g U, U = (D - d (d.D)) / |x - campos|, D = sum_k g_k dY_k/dd,
+// g_k = sum over unclamped channels c of w_c sh_kc (the grey weights w): the grey colour
+// is linear in the SH coefficients while no channel clamps, so the map's SH are folded
+// into U once in the forward.
+__device__ __forceinline__ void write_fcache(float4 *dst, const Pre &o, const float *cov, const float *sh,
+                                             int sh_degree, bool has_col)
+{
+    float T0S[3], T1S[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const float Sj[3] = {cov[j == 0 ? 0 : (j == 1 ? 1 : 2)], cov[j == 0 ? 1 : (j == 1 ? 3 : 4)],
+                             cov[j == 0 ? 2 : (j == 1 ? 4 : 5)]};
+        T0S[j] = o.T0[0] * Sj[0] + o.T0[1] * Sj[1] + o.T0[2] * Sj[2];
+        T1S[j] = o.T1[0] * Sj[0] + o.T1[1] * Sj[1] + o.T1[2] * Sj[2];
+    }
+    float U[3] = {0.0f, 0.0f, 0.0f};
+    if (!has_col) {
+        const float wc[3] = {o.rgb_raw[0] < 0.0f ? 0.0f : 0.2989f, o.rgb_raw[1] < 0.0f ? 0.0f : 0.587f,
+                             o.rgb_raw[2] < 0.0f ? 0.0f : 0.114f};
+        float gk[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) gk[k] = wc[0] * sh[3 * k] + wc[1] * sh[3 * k + 1] + wc[2] * sh[3 * k + 2];
+        float D[3];
+        sh_dir_grad(sh_degree, gk, o.dir[0], o.dir[1], o.dir[2], D);
+        const float dd = o.dir[0] * D[0] + o.dir[1] * D[1] + o.dir[2] * D[2];
+        const float il = 1.0f / o.dirlen;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) U[j] = (D[j] - o.dir[j] * dd) * il;
+    }
+    dst[0] = make_float4(o.cov2[0], o.cov2[1], o.cov2[2], o.det);
+    dst[1] = make_float4(T0S[0], T0S[1], T0S[2], T1S[0]);
+    dst[2] = make_float4(T1S[1], T1S[2], o.J[0], o.J[1]);
+    dst[3] = make_float4(o.J[2], o.J[3], o.pc[0], o.pc[1]);
+    dst[4] = make_float4(o.pc[2], o.pw, o.hom[0], o.hom[1]);
+    dst[5] = make_float4(U[0], U[1], U[2], __int_as_float((o.clampx ? 1 : 0) | (o.clampy ? 2 : 0)));
+}
+
 struct FwdParams {
     const gsevt_view *views;
     const gsevt_map *maps;
@@ -233,7 +278,7 @@ struct FwdParams {
     int32_t *radii;
 };
 
-__global__ void __launch_bounds__(GS_BLOCK) k_preprocess_fwd(FwdParams p)
+__global__ void __launch_bounds__(GS_BLOCK, 2) k_preprocess_fwd(FwdParams p)
 {
     __shared__ gsevt_map M;
     __shared__ gsevt_view V;
@@ -264,6 +309,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_preprocess_fwd(FwdParams p)
                 p.ws.recA[vg] = make_float4(o.mean[0], o.mean[1], o.pc[2], grey);
                 p.ws.recB[vg] = make_float4(o.conic[0], o.conic[1], o.conic[2], a.opac);
                 if (p.rgb) p.ws.recC[vg] = make_float4(o.rgb[0], o.rgb[1], o.rgb[2], 0.0f);
+                if (p.ws.fcache) write_fcache(p.ws.fcache + vg * GS_FCACHE, o, a.cov, a.sh, M.sh_degree, a.has_col);
             } else {
                 p.ws.bin[vg] = make_int4(0, 0, 0, 0);
             }
@@ -318,6 +364,7 @@ struct BwdParams {
     const gsevt_view *views;
     const gsevt_map *maps;
     int num_maps;
+    int num_views;
     int rgb;
     Workspace ws;
     const gsevt_map_grads *grads;  // device array [num_maps] or nullptr
@@ -594,6 +641,108 @@ __global__ void __launch_bounds__(GS_BLOCK, MAPGRAD ? 1 : 2) k_preprocess_bwd(Bw
     }
 }
 
+// Twist-only adjoint of the batched tracker from the forward cache: one thread per
+// (view, Gaussian) slot, block b = (view, chunk b - sb_offset), no map attributes and no
+// forward recomputation.  The chain is that of slot_backward for a grey frame without
+// map gradients, with S T0^T, S T1^T and the direction term U taken from the cache.
+__global__ void __launch_bounds__(GS_BLOCK) k_preprocess_bwd_cached(BwdParams p)
+{
+    __shared__ gsevt_view V;
+    __shared__ int s_n;
+    __shared__ double wpart[GS_BLOCK / 32][6];
+    const int b = blockIdx.x;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = p.num_views - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (p.views[mid].sb_offset <= b) lo = mid; else hi = mid - 1;
+        }
+        V = p.views[lo];
+        s_n = p.maps[V.map].n;
+    }
+    __syncthreads();
+    float xi[6] = {0, 0, 0, 0, 0, 0};
+    const int g = (b - V.sb_offset) * GS_BLOCK + threadIdx.x;
+    const size_t vg = (size_t)V.vg_offset + g;
+    if (g < s_n && p.ws.bin[vg].x > 0) {
+        const float4 *c = p.ws.fcache + vg * GS_FCACHE;
+        const float4 c0 = c[0], c1 = c[1], c2 = c[2], c3 = c[3], c4 = c[4], c5 = c[5];
+        const float4 GA = p.ws.gradA[vg], GB = p.ws.gradB[vg];
+        const float gCa = GA.z, gCb = GA.w, gCc = GB.x;
+        const float a2 = c0.x, b2 = c0.y, c2_ = c0.z, det = c0.w;
+        const float d2 = det * det;
+        const float ga = (gCa * (-c2_ * c2_) + gCb * (b2 * c2_) + gCc * (-b2 * b2)) / d2;
+        const float gb_ = (gCa * (2.0f * b2 * c2_) + gCb * (-(a2 * c2_ + b2 * b2)) + gCc * (2.0f * a2 * b2)) / d2;
+        const float gc = (gCa * (-b2 * b2) + gCb * (a2 * b2) + gCc * (-a2 * a2)) / d2;
+        const float Gs00 = ga, Gs01 = 0.5f * gb_, Gs11 = gc;
+        const float T0S[3] = {c1.x, c1.y, c1.z}, T1S[3] = {c1.w, c2.x, c2.y};
+        float gT0[3], gT1[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            gT0[j] = 2.0f * (Gs00 * T0S[j] + Gs01 * T1S[j]);
+            gT1[j] = 2.0f * (Gs01 * T0S[j] + Gs11 * T1S[j]);
+        }
+        const float *R = V.R;
+        const float J00 = c2.z, J02 = c2.w, J11 = c3.x, J12 = c3.y;
+        float gJ00 = 0, gJ02 = 0, gJ11 = 0, gJ12 = 0;
+        float gW[3][3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            gJ00 += gT0[j] * R[j];
+            gJ02 += gT0[j] * R[6 + j];
+            gJ11 += gT1[j] * R[3 + j];
+            gJ12 += gT1[j] * R[6 + j];
+            gW[0][j] = gT0[j] * J00;
+            gW[1][j] = gT1[j] * J11;
+            gW[2][j] = gT0[j] * J02 + gT1[j] * J12;
+        }
+        const float fx = (float)V.width / (2.0f * V.tanfovx), fy = (float)V.height / (2.0f * V.tanfovy);
+        const float vx = c3.z, vy = c3.w, vz = c4.x;
+        const float ivz = 1.0f / vz, ivz2 = ivz * ivz, ivz3 = ivz2 * ivz;
+        const int flags = __float_as_int(c5.w);
+        float gpc[3] = {0, 0, 0};
+        gpc[2] += gJ00 * (-fx * ivz2) + gJ11 * (-fy * ivz2);
+        if (!(flags & 1)) { gpc[0] += gJ02 * (-fx * ivz2); gpc[2] += gJ02 * (2.0f * fx * vx * ivz3); }
+        else { gpc[2] += gJ02 * (-J02 * ivz); }
+        if (!(flags & 2)) { gpc[1] += gJ12 * (-fy * ivz2); gpc[2] += gJ12 * (2.0f * fy * vy * ivz3); }
+        else { gpc[2] += gJ12 * (-J12 * ivz); }
+        const float gnx = GA.x * 0.5f * (float)V.width, gny = GA.y * 0.5f * (float)V.height;
+        const float pw = c4.y;
+        const float gh0 = gnx * pw, gh1 = gny * pw, gh3 = -(gnx * c4.z + gny * c4.w) * pw * pw;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) gpc[j] += V.P[j] * gh0 + V.P[4 + j] * gh1 + V.P[12 + j] * gh3;
+        gpc[2] += GB.w;
+        const float gu[3] = {GB.z * c5.x, GB.z * c5.y, GB.z * c5.z};
+        const float Rgu0 = R[0] * gu[0] + R[1] * gu[1] + R[2] * gu[2];
+        const float Rgu1 = R[3] * gu[0] + R[4] * gu[1] + R[5] * gu[2];
+        const float Rgu2 = R[6] * gu[0] + R[7] * gu[1] + R[8] * gu[2];
+        xi[0] = gpc[0] + Rgu0;
+        xi[1] = gpc[1] + Rgu1;
+        xi[2] = gpc[2] + Rgu2;
+        const float M12 = R[3] * gW[2][0] + R[4] * gW[2][1] + R[5] * gW[2][2];
+        const float M21 = R[6] * gW[1][0] + R[7] * gW[1][1] + R[8] * gW[1][2];
+        const float M20 = R[6] * gW[0][0] + R[7] * gW[0][1] + R[8] * gW[0][2];
+        const float M02 = R[0] * gW[2][0] + R[1] * gW[2][1] + R[2] * gW[2][2];
+        const float M01 = R[0] * gW[1][0] + R[1] * gW[1][1] + R[2] * gW[1][2];
+        const float M10 = R[3] * gW[0][0] + R[4] * gW[0][1] + R[5] * gW[0][2];
+        xi[3] = (vy * gpc[2] - vz * gpc[1]) + (M12 - M21);
+        xi[4] = (vz * gpc[0] - vx * gpc[2]) + (M20 - M02);
+        xi[5] = (vx * gpc[1] - vy * gpc[0]) + (M01 - M10);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        float sm = warp_sum(xi[k]);
+        if ((threadIdx.x & 31) == 0) wpart[threadIdx.x >> 5][k] = (double)sm;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double sm = 0.0;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) sm += wpart[w][threadIdx.x];
+        const float hi = (float)sm, lo = (float)(sm - (double)hi);
+        ((float2 *)p.ws.xi_part)[(size_t)b * 6 + threadIdx.x] = make_float2(hi, lo);
+    }
+}
+
 // per view: xi[v] = sum over the view's scan blocks of xi_part, in a fixed order (FP64)
 __global__ void k_xi_reduce(const gsevt_view *views, const gsevt_map *maps, Workspace ws, int num_views,
                             double *xi_out)
@@ -640,6 +789,23 @@ int gs_launch_preprocess_fwd(const gsevt_frame *f, const Workspace &ws, cudaStre
     return GSEVT_OK;
 }
 
+int gs_launch_preprocess_bwd_cached(const gsevt_frame *f, const Workspace &ws, cudaStream_t s)
+{
+    if (!ws.fcache) return GSEVT_ERR_ARG;
+    BwdParams p;
+    p.views = f->views;
+    p.maps = f->maps;
+    p.num_maps = f->L.num_maps;
+    p.num_views = f->L.num_views;
+    p.rgb = 0;
+    p.ws = ws;
+    p.grads = nullptr;
+    if (f->L.num_scan_blocks <= 0) return GSEVT_OK;
+    k_preprocess_bwd_cached<<<f->L.num_scan_blocks, GS_BLOCK, 0, s>>>(p);
+    GS_CUDA_CHECK();
+    return GSEVT_OK;
+}
+
 // reduce = false leaves the per-view sums to the caller (the batched tracker's finalize
 // kernel reduces the partials itself)
 int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gsevt_map_grads *grads_dev,
@@ -649,6 +815,7 @@ int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gs
     p.views = f->views;
     p.maps = f->maps;
     p.num_maps = f->L.num_maps;
+    p.num_views = f->L.num_views;
     p.rgb = f->L.channels == 3;
     p.ws = ws;
     p.grads = grads_dev;

@@ -150,7 +150,8 @@ EXPORTED = [
 WORKSPACE_REGIONS = ["status", "bin", "recA", "recB", "recC", "gradA", "gradB", "gradC", "vis_sums",
                      "vis_offs", "dkeys0", "dkeys1", "dvals0", "dvals1", "tsums", "toffs", "keys0", "keys1",
                      "vals0", "vals1", "sort_hist", "sort_counter", "sort_lookback", "ranges", "loss_part",
-                     "loss_scal", "loss_done", "xi_part", "xi", "csums", "coffs", "soffs", "sranges"]
+                     "loss_scal", "loss_done", "xi_part", "xi", "csums", "coffs", "soffs", "sranges",
+                     "fcache"]
 
 
 def workspace_offsets(layout):

@@ -164,10 +164,10 @@ void gsevt_abi_sizes(int32_t *out7);
  * tools), in this order: status, bin, recA, recB, recC, gradA, gradB, gradC, vis_sums,
  * vis_offs, dkeys0, dkeys1, dvals0, dvals1, tsums, toffs, keys0, keys1, vals0, vals1,
  * sort_hist, sort_counter, sort_lookback, ranges, loss_part, loss_scal, loss_done,
- * xi_part, xi, csums, coffs, soffs, sranges (33 entries; absent regions are reported
- * as UINT64_MAX).  keys are 32-bit global tile ids, vals 32-bit (view, Gaussian)
+ * xi_part, xi, csums, coffs, soffs, sranges, fcache (34 entries; absent regions are
+ * reported as UINT64_MAX).  keys are 32-bit global tile ids, vals 32-bit (view, Gaussian)
  * slots.  Touches no GPU state. */
-void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out33);
+void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out34);
 
 /* ---- map packing ----
  * Replaces the per-call activation + torch.cat of get_features
