@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(GS_BLOCK, MAPGRAD ? 1 : 2) k_preprocess_bwd(Bw
 {
     __shared__ gsevt_map M;
     __shared__ gsevt_view V;
-    __shared__ double wpart[GS_BLOCK / 32][6];
+    __shared__ float wpart[GS_BLOCK / 32][6];
     int b = blockIdx.x;
     if (threadIdx.x == 0) M = p.maps[gs_find_map(p.maps, p.num_maps, b)];
     __syncthreads();
@@ -576,20 +576,18 @@ __global__ void __launch_bounds__(GS_BLOCK, MAPGRAD ? 1 : 2) k_preprocess_bwd(Bw
                 gcov[3] += gS11; gcov[4] += 2.0f * gS12; gcov[5] += gS22;
             }
         }
-        // reduce the view's twist gradient: FP32 within the warp, FP64 across warps
+        // reduce the view's twist gradient: FP32 within the warp, the warp sums added as a
+        // float pair (error-free FP32 additions), stored unevaluated as (hi, lo)
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-            float s = warp_sum(xi[k]);
-            if ((threadIdx.x & 31) == 0) wpart[threadIdx.x >> 5][k] = (double)s;
+            const float sm = warp_sum(xi[k]);
+            if ((threadIdx.x & 31) == 0) wpart[threadIdx.x >> 5][k] = sm;
         }
         __syncthreads();
         if (threadIdx.x < 6) {
-            double s = 0.0;
-            for (int w = 0; w < GS_BLOCK / 32; ++w) s += wpart[w][threadIdx.x];
-            // stored as an unevaluated float pair hi + lo (48 significant bits), which
-            // the per-view sums can add with FP32 error-free transformations
-            const float hi = (float)s, lo = (float)(s - (double)hi);
-            ((float2 *)p.ws.xi_part)[(size_t)(V.sb_offset + gb) * 6 + threadIdx.x] = make_float2(hi, lo);
+            FP2 sm;
+            for (int w = 0; w < GS_BLOCK / 32; ++w) sm.add(wpart[w][threadIdx.x], 0.0f);
+            ((float2 *)p.ws.xi_part)[(size_t)(V.sb_offset + gb) * 6 + threadIdx.x] = make_float2(sm.hi, sm.lo);
         }
     }
     if (MAPGRAD && valid && p.grads) {
@@ -649,7 +647,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_preprocess_bwd_cached(BwdParams p)
 {
     __shared__ gsevt_view V;
     __shared__ int s_n;
-    __shared__ double wpart[GS_BLOCK / 32][6];
+    __shared__ float wpart[GS_BLOCK / 32][6];
     const int b = blockIdx.x;
     if (threadIdx.x == 0) {
         int lo = 0, hi = p.num_views - 1;
@@ -729,17 +727,18 @@ __global__ void __launch_bounds__(GS_BLOCK) k_preprocess_bwd_cached(BwdParams p)
         xi[4] = (vz * gpc[0] - vx * gpc[2]) + (M20 - M02);
         xi[5] = (vx * gpc[1] - vy * gpc[0]) + (M01 - M10);
     }
+    // FP32 within the warp, the eight warp sums added as a float pair (error-free FP32
+    // additions, no FP64 arithmetic) in warp order
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        float sm = warp_sum(xi[k]);
-        if ((threadIdx.x & 31) == 0) wpart[threadIdx.x >> 5][k] = (double)sm;
+        const float sm = warp_sum(xi[k]);
+        if ((threadIdx.x & 31) == 0) wpart[threadIdx.x >> 5][k] = sm;
     }
     __syncthreads();
     if (threadIdx.x < 6) {
-        double sm = 0.0;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) sm += wpart[w][threadIdx.x];
-        const float hi = (float)sm, lo = (float)(sm - (double)hi);
-        ((float2 *)p.ws.xi_part)[(size_t)b * 6 + threadIdx.x] = make_float2(hi, lo);
+        FP2 sm;
+        for (int w = 0; w < GS_BLOCK / 32; ++w) sm.add(wpart[w][threadIdx.x], 0.0f);
+        ((float2 *)p.ws.xi_part)[(size_t)b * 6 + threadIdx.x] = make_float2(sm.hi, sm.lo);
     }
 }
 
