@@ -435,12 +435,16 @@ __global__ void __launch_bounds__(FILTER_WARPS * 32) k_filter_tiles(const gsevt_
         uint32_t base = 0;
         if (lane == FILTER_TILES - 1) base = atomicAdd(ws.status + 7, inc);
         base = __shfl_sync(0xffffffffu, base, FILTER_TILES - 1);
+        const uint32_t total = __shfl_sync(0xffffffffu, inc, FILTER_TILES - 1);
+        // a region past the fine-list capacity (the key count has flagged the overflow)
+        // gets empty ranges, so that no reader goes past the buffer
+        const bool fits = (uint64_t)base + total <= (uint64_t)capacity;
         if (lane < FILTER_TILES) {
             const uint32_t start = base + inc - tot;
             s_start[lane] = start;
             const int tx = X + (lane % GS_SUPER), ty = Y + (lane / GS_SUPER);
             if (tx < V.tiles_x && ty < V.tiles_y)
-                ws.ranges[V.tile_offset + ty * V.tiles_x + tx] = make_uint2(start, start + tot);
+                ws.ranges[V.tile_offset + ty * V.tiles_x + tx] = fits ? make_uint2(start, start + tot) : make_uint2(0, 0);
         }
     }
     __syncthreads();

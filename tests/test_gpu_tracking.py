@@ -131,6 +131,24 @@ def test_super_tile_lists_match_tile_sort(sizes):
     assert torch.equal(img_c, fr.image)
 
 
+def test_super_tile_overflow_is_reported_not_faulting():
+    """A key capacity far below the frame's pairs: the batched step flags the overflow,
+    keeps every write and every tile range inside the buffers, and the GPU stays usable."""
+    s0, pk0, sig0, _, _ = _scenario(20000, 320, 240, 300.0, 5, 30000)
+    R, t = synthetic.perturb(s0.gt_R, s0.gt_t, np.random.default_rng(3), 0.05, 3.0)
+    c = s0.camera
+    prob = Problem(0, R, t, s0.init_lin, s0.init_ang, s0.delta_tau, c.width, c.height, c.fx, c.fy,
+                   sig0[0].reshape(-1), opt_vel=True)
+    bt = BatchedTracker([{"packed": pk0, "n": 20000}], [prob], key_capacity=1000, device=DEV)
+    bt.step()
+    torch.cuda.synchronize()
+    st, k = bt.frame.status()
+    assert k > 1000 and st & _lib.STATUS_KEY_OVERFLOW and not st & _lib.STATUS_SORT_TIMEOUT
+    T = bt.frame.L.total_tiles
+    rng = _ws_region(bt.frame, "ranges", torch.int32, 2 * T).view(T, 2).cpu().numpy()
+    assert (rng[:, 1] >= rng[:, 0]).all() and rng.max() <= 1000
+
+
 def test_batched_converges_like_plain():
     """100 fine-stage Adam iterations from a 5 cm / 3 degree perturbation: the batched
     adjoint path and the plain per-view drop-in path end within 1 mm / 0.05 degrees."""
