@@ -553,7 +553,7 @@ def main():
     # preprocess bwd, finalize
     L = bt.frame.L
     super_bits = max(1, int(L.total_tiles // 4 + L.num_views).bit_length())
-    launches_per_iter = 18 + (super_bits + 7) // 8
+    launches_per_iter = 19 + (super_bits + 7) // 8
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
