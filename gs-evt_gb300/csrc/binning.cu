@@ -134,6 +134,11 @@ __global__ void __launch_bounds__(GS_BLOCK) k_compact(BinParams p)
     if (vis) {
         p.ws.dkeys[0][c] = (uint32_t)bin.w;
         p.ws.dvals[0][c] = (uint32_t)vg;
+        // the adjoint blend accumulates into these with atomics: clear them here, in slot
+        // order (coalesced), for every slot that can receive a contribution
+        p.ws.gradA[vg] = make_float4(0, 0, 0, 0);
+        p.ws.gradB[vg] = make_float4(0, 0, 0, 0);
+        if (p.rgb) p.ws.gradC[vg] = make_float4(0, 0, 0, 0);
     }
 }
 
@@ -163,6 +168,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sorted_sums(BinParams p, const uin
             int sx0, sy0, sx1, sy1;
             super_rect(b, sx0, sy0, sx1, sy1);
             scnt = (uint32_t)((sx1 - sx0) * (sy1 - sy0));
+        }
+        if (COARSE) {
+            // the slot's tile rectangle in depth order (the depth sort's second buffers are
+            // free), so that the coarse duplication reads it coalesced
+            p.ws.dkeys[1][i] = (uint32_t)b.y;
+            p.ws.dvals[1][i] = (uint32_t)b.z;
         }
     }
 #pragma unroll
@@ -220,9 +231,6 @@ __global__ void __launch_bounds__(GS_BLOCK) k_duplicate(BinParams p, const uint3
     const uint32_t off = p.ws.toffs[blockIdx.x] + block_excl_scan(cnt, wtot);
     int x0 = 0, y0 = 0, rw = 1, toff = 0, tpx = 1;
     if (cnt > 0) {
-        p.ws.gradA[vg] = make_float4(0, 0, 0, 0);
-        p.ws.gradB[vg] = make_float4(0, 0, 0, 0);
-        if (p.rgb) p.ws.gradC[vg] = make_float4(0, 0, 0, 0);
         const gsevt_view &V = p.views[find_view_by_vg(p.views, p.num_views, vg)];
         x0 = bin.y & 0xffff;
         y0 = (bin.y >> 16) & 0xffff;
@@ -277,14 +285,11 @@ __global__ void __launch_bounds__(GS_BLOCK) k_duplicate_coarse(BinParams p, cons
     int4 bin = make_int4(0, 0, 0, 0);
     if (i < nvis) {
         vg = sorted_vals[i];
-        bin = p.ws.bin[vg];
+        bin = make_int4(1, (int)p.ws.dkeys[1][i], (int)p.ws.dvals[1][i], 0);  // visible: touches >= 1 tile
     }
     int sx0 = 0, sy0 = 0, srw = 1, soff = 0, stx = 1;
     uint32_t cnt = 0;
     if (bin.x > 0) {
-        p.ws.gradA[vg] = make_float4(0, 0, 0, 0);
-        p.ws.gradB[vg] = make_float4(0, 0, 0, 0);
-        if (p.rgb) p.ws.gradC[vg] = make_float4(0, 0, 0, 0);
         const int v = find_view_by_vg(p.views, p.num_views, vg);
         const gsevt_view &V = p.views[v];
         int sx1, sy1;
