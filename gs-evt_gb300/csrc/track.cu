@@ -179,9 +179,9 @@ __device__ inline void write_view_pose(gsevt_view *V, const float *R, const floa
 
 // One block per pose.  The block sums the per-scan-block twist partials of the pose's two
 // views as float pairs with error-free FP32 transformations (about 48 significant bits;
-// GB300's FP64 rate would make plain double sums the slowest part of the kernel): thread
-// i adds partials i, i + 256, ... in order, four loads in flight, then warp and block
-// combinations in a fixed order.  The pose state is staged in shared memory.  Warp 0 then runs the serial part with its lanes sharing the
+// GB300's FP64 rate would make plain double sums the slowest part of the kernel): each
+// view by half of the block, thread i adding partials i, i + 128, ... in order, four loads
+// in flight, then warp and block combinations in a fixed order.  The pose state is staged in shared memory.  Warp 0 then runs the serial part with its lanes sharing the
 // independent pieces: the two views' chain terms (lanes 0, 1), the four Adam groups
 // (lanes 0-3), the pose update (lane 0) and the two view rewrites (lanes 0, 1).
 __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, const gsevt_map *maps,
@@ -200,16 +200,19 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
         ((uint32_t *)&S)[i] = ((const uint32_t *)(poses + pi))[i];
     __syncthreads();
     const int vids[2] = {S.last_view, S.next_view};
-    for (int k = 0; k < 2; ++k) {
+    {
+        // the two views are reduced concurrently, each by half of the block
+        constexpr int HALF = GS_BLOCK / 2;
+        const int k = threadIdx.x / HALF, t = threadIdx.x % HALF;
         const gsevt_view &V = views[vids[k]];
         const int nb = (maps[V.map].n + GS_BLOCK - 1) / GS_BLOCK;
         const float2 *xp = (const float2 *)ws.xi_part + (size_t)V.sb_offset * 6;
         FP2 acc[6];
-        for (int i0 = threadIdx.x; i0 < nb; i0 += 4 * GS_BLOCK) {
+        for (int i0 = t; i0 < nb; i0 += 4 * HALF) {
             float2 x[4][6];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const int i = i0 + j * GS_BLOCK;
+                const int i = i0 + j * HALF;
 #pragma unroll
                 for (int q = 0; q < 6; ++q) x[j][q] = i < nb ? xp[(size_t)i * 6 + q] : make_float2(0.0f, 0.0f);
             }
@@ -232,14 +235,14 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
                 a.add(b2.hi, b2.lo);
                 sm = a;
             }
-            if ((threadIdx.x & 31) == 0) part[k][threadIdx.x >> 5][q] = make_float2(sm.hi, sm.lo);
+            if ((t & 31) == 0) part[k][t >> 5][q] = make_float2(sm.hi, sm.lo);
         }
     }
     __syncthreads();
     if (threadIdx.x < 12) {
         const int k = threadIdx.x / 6, q = threadIdx.x % 6;
         FP2 sm;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) sm.add(part[k][w][q].x, part[k][w][q].y);
+        for (int w = 0; w < GS_BLOCK / 64; ++w) sm.add(part[k][w][q].x, part[k][w][q].y);
         const double v = (double)sm.hi + (double)sm.lo;
         ws.xi[6 * vids[k] + q] = v;
         s_g[k][q] = (float)v;
@@ -333,24 +336,32 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
             }
         }
         __syncwarp();
-        if (lane == 0) {
-            // update_vwRT: velocity first, then the pose
-            if (S.opt_vel)
-                for (int k = 0; k < 3; ++k) { S.ang_vel[k] += s_delta[6 + k]; S.lin_vel[k] += s_delta[9 + k]; }
+        {
+            // update_pose: T <- SE3_exp([rho, theta]) T, the FP64 product spread over lanes
+            // 0-11 (one entry each; every lane forms the same FP32 exponential)
             float xi[6] = {s_delta[3], s_delta[4], s_delta[5], s_delta[0], s_delta[1], s_delta[2]};
             M3 Rd;
             float td[3];
             se3_exp(xi, Rd, td);
-            double Rn[9], tn[3];
-            for (int i = 0; i < 3; ++i) {
-                for (int j = 0; j < 3; ++j)
-                    Rn[3 * i + j] = (double)Rd.a[3 * i] * S.R[j] + (double)Rd.a[3 * i + 1] * S.R[3 + j] +
-                                    (double)Rd.a[3 * i + 2] * S.R[6 + j];
-                tn[i] = (double)Rd.a[3 * i] * S.t[0] + (double)Rd.a[3 * i + 1] * S.t[1] +
-                        (double)Rd.a[3 * i + 2] * S.t[2] + (double)td[i];
+            double nv = 0.0;
+            if (lane < 9) {
+                const int i = lane / 3, j = lane % 3;
+                nv = (double)Rd.a[3 * i] * S.R[j] + (double)Rd.a[3 * i + 1] * S.R[3 + j] +
+                     (double)Rd.a[3 * i + 2] * S.R[6 + j];
+            } else if (lane < 12) {
+                const int i = lane - 9;
+                nv = (double)Rd.a[3 * i] * S.t[0] + (double)Rd.a[3 * i + 1] * S.t[1] +
+                     (double)Rd.a[3 * i + 2] * S.t[2] + (double)td[i];
             }
-            for (int i = 0; i < 9; ++i) S.R[i] = Rn[i];
-            for (int i = 0; i < 3; ++i) S.t[i] = tn[i];
+            __syncwarp();
+            if (lane < 9) S.R[lane] = nv;
+            else if (lane < 12) S.t[lane - 9] = nv;
+            __syncwarp();
+        }
+        if (lane == 0) {
+            // update_vwRT: velocity first (the pose update above uses only the deltas)
+            if (S.opt_vel)
+                for (int k = 0; k < 3; ++k) { S.ang_vel[k] += s_delta[6 + k]; S.lin_vel[k] += s_delta[9 + k]; }
             S.iter += 1;
             if (S.control) {
                 // losses.append(loss); converged = mean |diff(last 11 losses)| < threshold
