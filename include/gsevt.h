@@ -304,7 +304,13 @@ typedef struct gsevt_pose_state {
     double hist[11];             /* last 11 losses of this level (ring) */
 } gsevt_pose_state;
 
-/* poses: device array.  Pair p's loss goes to loss_out[p] (device, nullable). */
+/* poses: device array.  Pair p's loss goes to loss_out[p] (device, nullable).
+ * The frame must be grey (channels == 1) with render pairs; its workspace then carries
+ * the forward cache the twist-only adjoint reads.  Binning goes through 4x4-tile
+ * super-tiles and yields the same per-tile lists as gsevt_bin_and_sort (depth order,
+ * ties in slot order); the key capacity bounds the (tile, Gaussian) pairs as there, and
+ * an overflow is flagged in the status words with every tile range left inside the
+ * buffers.  Call gsevt_track_init_views once before the first step. */
 int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *poses, int32_t num_poses,
                              double *loss_out, gsevt_stream_t stream);
 /* Write the two view entries (pose R, t, campos) of every pose from its state; the
