@@ -269,6 +269,41 @@ __device__ __forceinline__ void write_fcache(float4 *dst, const Pre &o, const fl
     dst[5] = make_float4(U[0], U[1], U[2], __int_as_float((o.clampx ? 1 : 0) | (o.clampy ? 2 : 0)));
 }
 
+// Batched-tracker frames (those with the adjoint cache) bin a Gaussian only into the
+// tiles that its alpha support can reach: the reference's 3-sigma tile rectangle is
+// intersected with the tiles holding pixels of a conservative box of the support.  A
+// pixel blends the Gaussian only if alpha = min(0.99, o exp(power)) >= 1/255, i.e.
+// -power <= tau = ln(255 o); in exact arithmetic -power = d^T M d / 2 for the conic M, and
+// the FP32 evaluation deviates by less than 1e-6 tr(M) |d|^2, so every such pixel lies in
+// the box of d^T (M/2 - 1e-6 tr(M) I) d <= tau (1 + 1e-4) + 1e-3, widened by 0.1 % + 0.5
+// px.  Dropped tiles hold no pixel that could blend the Gaussian, so every tile's image,
+// transmittance and gradients are unchanged; only the per-tile list indices (contributor
+// counts, which these frames do not output) differ from the full rectangle's.
+__device__ __forceinline__ void tighten_rect(Pre &o, float opac, const gsevt_view &V)
+{
+    if (!(opac >= (1.0f / 255.0f) * 0.999f)) {  // no pixel can pass the alpha test
+        o.rect[2] = o.rect[0];
+        return;
+    }
+    const float tau = logf(255.0f * opac) * 1.0001f + 1e-3f;
+    const float Bx = o.conic[0], By = o.conic[1], Bz = o.conic[2];
+    const float g = 1e-6f * (fabsf(Bx) + fabsf(Bz));
+    const float a = 0.5f * Bx - g, b = 0.5f * By, c = 0.5f * Bz - g;
+    const float det = a * c - b * b;
+    if (!(a > 0.0f && c > 0.0f && det > 0.0f && tau > -1e29f && tau < 1e29f)) return;  // keep the rectangle
+    const float hx = sqrtf(fmaxf(tau, 0.0f) * c / det) * 1.001f + 0.5f;
+    const float hy = sqrtf(fmaxf(tau, 0.0f) * a / det) * 1.001f + 0.5f;
+    const float gx = (float)V.tiles_x, gy = (float)V.tiles_y;
+    const int bx0 = (int)fminf(gx, fmaxf(0.0f, floorf((o.mean[0] - hx) * (1.0f / 16.0f))));
+    const int bx1 = (int)fminf(gx, fmaxf(0.0f, floorf((o.mean[0] + hx) * (1.0f / 16.0f)) + 1.0f));
+    const int by0 = (int)fminf(gy, fmaxf(0.0f, floorf((o.mean[1] - hy) * (1.0f / 16.0f))));
+    const int by1 = (int)fminf(gy, fmaxf(0.0f, floorf((o.mean[1] + hy) * (1.0f / 16.0f)) + 1.0f));
+    o.rect[0] = max(o.rect[0], bx0);
+    o.rect[1] = max(o.rect[1], by0);
+    o.rect[2] = min(o.rect[2], bx1);
+    o.rect[3] = min(o.rect[3], by1);
+}
+
 struct FwdParams {
     const gsevt_view *views;
     const gsevt_map *maps;
@@ -301,6 +336,8 @@ __global__ void __launch_bounds__(GS_BLOCK, 2) k_preprocess_fwd(FwdParams p)
             Pre o;
             bool vis = pre_forward(a.xyz, a.cov, a.sh, M.sh_degree, a.has_col ? a.col : nullptr, V, o);
             size_t vg = (size_t)V.vg_offset + g;
+            if (vis && p.ws.fcache) tighten_rect(o, a.opac, V);
+            vis = vis && o.rect[2] > o.rect[0] && o.rect[3] > o.rect[1];
             if (vis) {
                 touched = (uint32_t)((o.rect[2] - o.rect[0]) * (o.rect[3] - o.rect[1]));
                 float grey = grey_of(o.rgb);

@@ -149,6 +149,34 @@ def test_super_tile_overflow_is_reported_not_faulting():
     assert (rng[:, 1] >= rng[:, 0]).all() and rng.max() <= 1000
 
 
+def test_batched_step_with_a_problem_that_sees_nothing():
+    """A problem whose camera faces away from the map (no visible Gaussian, empty super-tile
+    groups, zero pairs) batched with a normal one: the normal problem's loss and gradient
+    equal its single launch, the empty one's pose does not move, and nothing faults."""
+    s0, pk0, sig0, _, _ = _scenario(20000, 320, 240, 300.0, 9, 30000)
+    c = s0.camera
+    R, t = synthetic.perturb(s0.gt_R, s0.gt_t, np.random.default_rng(4), 0.05, 3.0)
+    flip = np.diag([-1.0, 1.0, -1.0])  # 180 degrees about the camera y axis
+    Rb, tb = flip @ s0.gt_R, flip @ s0.gt_t
+    good = Problem(0, R, t, s0.init_lin, s0.init_ang, s0.delta_tau, c.width, c.height, c.fx, c.fy,
+                   sig0[0].reshape(-1), opt_vel=True)
+    blind = Problem(0, Rb, tb, s0.init_lin, s0.init_ang, s0.delta_tau, c.width, c.height, c.fx, c.fy,
+                    sig0[0].reshape(-1), opt_vel=True)
+    maps = [{"packed": pk0, "n": 20000}]
+    bt = BatchedTracker(maps, [good, blind], device=DEV)
+    bt.step()
+    torch.cuda.synchronize()
+    st = bt.states()
+    single = BatchedTracker(maps, [good], device=DEV)
+    single.step()
+    ss = single.states()
+    assert ss["loss"][0] == st["loss"][0]
+    assert np.linalg.norm(ss["grad"][0] - st["grad"][0]) <= 1e-5 * np.linalg.norm(ss["grad"][0])
+    assert np.all(st["grad"][1] == 0.0)
+    np.testing.assert_allclose(st["R"][1], Rb, atol=1e-12)
+    np.testing.assert_allclose(st["t"][1], tb, atol=1e-12)
+
+
 def test_batched_converges_like_plain():
     """100 fine-stage Adam iterations from a 5 cm / 3 degree perturbation: the batched
     adjoint path and the plain per-view drop-in path end within 1 mm / 0.05 degrees."""
