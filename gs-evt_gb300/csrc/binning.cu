@@ -15,6 +15,12 @@
 // of the full (tile | depth) key sort - but the large array is sorted on 32-bit keys over
 // 2 passes instead of 64-bit keys over 6.
 // k_ranges: [start, end) of every global tile in the sorted pairs.
+//
+// The batched tracker replaces steps 4-5 by binning through 4x4-tile super-tiles:
+// k_duplicate_coarse writes one (super-tile, slot) pair per super-tile of the slot's rect
+// (4.6x fewer pairs), a stable sort by super-tile keeps each group in depth order, and
+// k_filter_tiles cuts every tile's list out of its super-tile's group, in order.  The
+// per-tile lists equal those of steps 4-5 (gs_launch_bin_coarse).
 #include "common.cuh"
 
 template <typename KT>

@@ -10,11 +10,16 @@
 // radius = ceil(3 sqrt(lambda_max)), 16x16 tile rect, SH degree-3 colour + 0.5 clamped
 // at 0, grey = 0.2989 R + 0.587 G + 0.114 B (utils/render_camera/frame.py:39-43).
 //
-// Adjoint (k_preprocess_bwd): same per-Gaussian/per-view loop; recomputes the forward
-// quantities, chains the blend adjoint's per-Gaussian 2D gradients through conic,
-// cov2D, the Jacobian, the projection, depth and the SH view direction to (a) the
-// left-twist gradient of each view (warp-reduced in FP32, block- and grid-reduced in
-// FP64) and (b) optionally the map gradients of the drop-in API.
+// For batched-tracker frames the forward also bins each Gaussian only into the tiles its
+// alpha support reaches (tighten_rect) and caches the per-slot intermediates of the
+// twist-only adjoint (write_fcache).
+//
+// Adjoint (k_preprocess_bwd, drop-in): same per-Gaussian/per-view loop; recomputes the
+// forward quantities, chains the blend adjoint's per-Gaussian 2D gradients through
+// conic, cov2D, the Jacobian, the projection, depth and the SH view direction to (a) the
+// left-twist gradient of each view (warp-reduced in FP32, block sums as float pairs,
+// per-view sums in FP64) and (b) optionally the map gradients of the drop-in API.
+// k_preprocess_bwd_cached is the batched tracker's twist-only adjoint from the cache.
 #include "common.cuh"
 
 namespace {
