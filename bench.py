@@ -475,6 +475,23 @@ def run_profile(args):
                       "keys": k, "status": st}))
 
 
+def max_over_ranks(x, device):
+    """Largest value of the float x over the ranks of the default process group (x when
+    there is none): the job's time is its slowest replica's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(per_rank_iters_per_s, world):
+    """Whole-job throughput of `world` independent replicas (weak scaling)."""
+    return per_rank_iters_per_s * world
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -522,18 +539,11 @@ def main():
     clocks.start()
     times = time_batched(bt, args.steps, warmup, flush)
     clk = clocks.stop()
-    ms = sum(times) / len(times)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(times) / len(times), dev)
     iters_per_s = 1000.0 / ms * bt.num
-    value = iters_per_s * world
+    value = replica_value(iters_per_s, world)
     e2e_ms, h2d, d2h = time_e2e(bt, prob, max(10, args.steps // 2), 3)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, dev)
     plain_ms = None if args.no_plain else time_plain(prob, dev)
     st, K = bt.check_status()
 
