@@ -13,11 +13,14 @@
 // per-pixel decisions and sums are bit-identical to the CPU oracle.
 //
 // Adjoint: the same front-to-back traversal with the same decisions (no per-pixel
-// contributor lists are stored); with P the running prefix of c alpha T and C the
-// stored pixel value,
-//   dC/dalpha_i = T_i c_i - (C - P_i + T_final bg) / (1 - alpha_i).
-// Per-Gaussian contributions are reduced across the warp in FP32 (shuffles), summed
-// per tile in shared memory and added to the global per-slot gradients once per tile.
+// contributor lists are stored); with P_i the running prefix of c alpha T up to and
+// including Gaussian i and C the stored pixel value (Gaussians plus T_final bg),
+//   dC/dalpha_i = T_i c_i - (C - P_i) / (1 - alpha_i).
+// The power's gradient enters the 2D mean and conic gradients linearly in the conic, so a
+// pixel contributes the five moments dpow (dx, dy, dx^2, dx dy, dy^2) and the conic is
+// applied once per Gaussian and tile.  Per-Gaussian contributions are reduced across the
+// warp in FP32 (shuffles), summed per tile in shared memory and added to the global
+// per-slot gradients once per tile.
 //
 // Warp-level culling (both directions): each batch Gaussian gets a conservative pixel
 // box and quadratic form of its alpha support (gauss_box); a warp ballots which of them
@@ -325,14 +328,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
     const int pix = V.pix_offset + py * V.width + px;
 
     // per-pixel inputs
-    float Tf = 1.0f, Cfg[3] = {0, 0, 0}, gC[3] = {0, 0, 0}, gD = 0.0f, gA = 0.0f, Dtot = 0.0f, Atot = 0.0f;
-    float bgc[3];
-    if (RGB) { bgc[0] = V.bg[0]; bgc[1] = V.bg[1]; bgc[2] = V.bg[2]; }
-    else { bgc[0] = (0.2989f * V.bg[0] + 0.587f * V.bg[1]) + 0.114f * V.bg[2]; bgc[1] = bgc[2] = 0.0f; }
+    // Cimg: the rendered pixel (Gaussians plus background); the colour behind the
+    // Gaussian at hand is Cimg minus the front-to-back partial sum Pc
+    float Cimg[3] = {0, 0, 0}, gC[3] = {0, 0, 0}, gD = 0.0f, gA = 0.0f, Dtot = 0.0f, Atot = 0.0f;
     if (inside) {
-        Tf = p.final_T[pix];
 #pragma unroll
-        for (int c = 0; c < (RGB ? 3 : 1); ++c) Cfg[c] = p.image[c * P + pix] - Tf * bgc[c];
+        for (int c = 0; c < (RGB ? 3 : 1); ++c) Cimg[c] = p.image[c * P + pix];
         if (MODE != 0) {
 #pragma unroll
             for (int c = 0; c < (RGB ? 3 : 1); ++c) gC[c] = p.dL_dimage[c * P + pix];
@@ -341,24 +342,23 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         } else if (V.pair >= 0) {
             // gradient of the pair loss w.r.t. this view's grey image
             const gsevt_pair &pr = p.pairs[V.pair];
-            const double *sc = p.ws.loss_scal + 4 * V.pair;
-            const double s = sc[0], cross = sc[1], L = sc[3];
+            const LossScal &sc = p.ws.loss_scal[V.pair];
+            const float inv_s = sc.inv_s, ng = sc.ndotg, inv_L = sc.inv_L;
             const int lp = py * V.width + px;
             const int other = V.pair_role == 0 ? pr.next_view : pr.last_view;
             const float Io = p.image[p.views[other].pix_offset + lp];
             const float Is = p.image[pix];
             const float dI = V.pair_role == 0 ? (Io - Is) : (Is - Io);
             const float e = (pr.unsigned_mode && pr.event_abs) ? pr.event_abs[lp] : pr.event[lp];
-            const float n = (float)((double)dI / s);
-            const float ng = (float)((1.0 - cross / s) / L);
+            const float n = dI * inv_s;
             float g;
             if (pr.unsigned_mode) {
                 const float sg = (dI > 0.0f) ? 1.0f : (dI < 0.0f ? -1.0f : 0.0f);
-                g = sg * (fabsf(n) - fabsf(e)) / (float)L;
+                g = sg * (fabsf(n) - fabsf(e)) * inv_L;
             } else {
-                g = (n - e) / (float)L;
+                g = (n - e) * inv_L;
             }
-            const float dd = (g - n * ng) / (float)s;
+            const float dd = (g - n * ng) * inv_s;
             gC[0] = V.pair_role == 0 ? -dd : dd;
         }
     }
@@ -426,27 +426,31 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                                 float dal = 0.0f;
 #pragma unroll
                                 for (int c = 0; c < (RGB ? 3 : 1); ++c) {
-                                    Pc[c] = Pc[c] + (col[c] * alpha) * T;
-                                    const float suffix = (Cfg[c] - Pc[c]) + Tf * bgc[c];
-                                    dal += gC[c] * (T * col[c] - suffix * inv1m);
+                                    Pc[c] = __fmaf_rn(col[c], wgt, Pc[c]);
+                                    const float suffix = Cimg[c] - Pc[c];
+                                    dal = __fmaf_rn(gC[c], __fmaf_rn(-suffix, inv1m, T * col[c]), dal);
                                 }
                                 if (MODE != 0) {
-                                    PD = PD + (A.z * alpha) * T;
-                                    PA = PA + alpha * T;
-                                    dal += gD * (T * A.z - (Dtot - PD) * inv1m);
-                                    dal += gA * (T - (Atot - PA) * inv1m);
+                                    PD = __fmaf_rn(A.z, wgt, PD);
+                                    PA = PA + wgt;
+                                    dal = __fmaf_rn(gD, __fmaf_rn(-(Dtot - PD), inv1m, T * A.z), dal);
+                                    dal = __fmaf_rn(gA, __fmaf_rn(-(Atot - PA), inv1m, T), dal);
                                     gv[7] = gD * wgt;
                                 }
                                 gv[6] = gC[0] * wgt;
                                 if (RGB) { gv[8] = gC[1] * wgt; gv[9] = gC[2] * wgt; }
                                 if (araw <= 0.99f) {
+                                    // d power / d(mean, conic) is linear in the conic: accumulate
+                                    // the moments of dpow over (dx, dy) and apply the conic once per
+                                    // Gaussian when the batch is flushed
                                     gv[5] = dal * G;
                                     const float dpow = dal * araw;
-                                    gv[2] = dpow * (-0.5f * dx * dx);
-                                    gv[3] = dpow * (-dx * dy);
-                                    gv[4] = dpow * (-0.5f * dy * dy);
-                                    gv[0] = dpow * (-B.x * dx - B.y * dy);
-                                    gv[1] = dpow * (-B.z * dy - B.y * dx);
+                                    const float mx = dpow * dx, my = dpow * dy;
+                                    gv[0] = mx;
+                                    gv[1] = my;
+                                    gv[2] = mx * dx;
+                                    gv[3] = mx * dy;
+                                    gv[4] = my * dy;
                                 }
                                 T = test_T;
                             }
@@ -469,6 +473,18 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         // flush this batch's per-Gaussian sums to the global per-slot gradients
         if ((int)threadIdx.x < n) {
             const uint32_t vg = cur.id[threadIdx.x];
+            // moments (sum dpow dx, dpow dy, dpow dx^2, dpow dx dy, dpow dy^2) to the
+            // gradients of the 2D mean and the conic
+            {
+                const float4 B = cur.B[threadIdx.x];
+                float *a = acc[threadIdx.x];
+                const float mx = a[0], my = a[1], mxx = a[2], mxy = a[3], myy = a[4];
+                a[0] = -(B.x * mx + B.y * my);
+                a[1] = -(B.z * my + B.y * mx);
+                a[2] = -0.5f * mxx;
+                a[3] = -mxy;
+                a[4] = -0.5f * myy;
+            }
             float *dst[10] = {(float *)(p.ws.gradA + vg), (float *)(p.ws.gradA + vg) + 1, (float *)(p.ws.gradA + vg) + 2,
                               (float *)(p.ws.gradA + vg) + 3, (float *)(p.ws.gradB + vg), (float *)(p.ws.gradB + vg) + 1,
                               (float *)(p.ws.gradB + vg) + 2, (float *)(p.ws.gradB + vg) + 3,

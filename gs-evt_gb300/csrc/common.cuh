@@ -55,6 +55,15 @@ __host__ __device__ __forceinline__ float gs_expf(float x)
 }
 
 // ------------------------------------------------------------ workspace ---------
+// Pair loss scalars.  With d = I_next - I_last, s = |d|, n = d / s and e the event
+// frame: cross = d . e (|d| . |e| in unsigned mode), e2 = e . e, L = |n - e|.  The
+// per-pixel image gradient is dL/dd = (g - n ndotg) / s with g = (n - e) / L
+// (sign(d) (|n| - |e|) / L in unsigned mode) and ndotg = n . g = (1 - cross / s) / L.
+struct LossScal {
+    double s, cross, e2, L;
+    float inv_s, ndotg, inv_L, pad;
+};
+
 struct Workspace {
     uint32_t *status;     // [0] status bits, [1] num keys, [2] last sort epoch, [4] sort epoch base,
                           // [5] number of visible (view, Gaussian) slots, [6] number of coarse
@@ -79,7 +88,7 @@ struct Workspace {
     unsigned long long *sort_lookback;  // [sort tiles][256]  {epoch:32 | flag:2 | count:30}
     uint2 *ranges;        // [total_tiles]
     double *loss_part;    // [loss_blocks][4]
-    double *loss_scal;    // [num_pairs][4] {s, cross, e2, L}
+    LossScal *loss_scal;  // [num_pairs] norms of the pair loss and the per-pixel gradient factors
     uint32_t *loss_done;  // [num_pairs]
     double *xi_part;      // [num_scan_blocks][6] float pairs (hi, lo) of the block's twist sums
     double *xi;           // [num_views][6]
@@ -160,7 +169,7 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     w.sort_lookback = (unsigned long long *)take((size_t)gs_lookback_tiles(L) * 256 * 8);
     w.ranges = (uint2 *)take((size_t)L.total_tiles * 8);
     w.loss_part = (double *)take((size_t)L.loss_blocks * 4 * 8);
-    w.loss_scal = (double *)take((size_t)L.num_pairs * 4 * 8);
+    w.loss_scal = (LossScal *)take((size_t)L.num_pairs * sizeof(LossScal));
     w.loss_done = (uint32_t *)take((size_t)L.num_pairs * 4);
     w.xi_part = (double *)take((size_t)L.num_scan_blocks * 6 * 8);
     w.xi = (double *)take((size_t)L.num_views * 6 * 8);

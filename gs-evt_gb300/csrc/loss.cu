@@ -8,7 +8,8 @@
 // so one reduction pass gives L (FP32 over each thread's 8 pixels, float pairs with
 // error-free additions within a block, FP64 across blocks); the per-pixel gradient
 //   dL/dI_next = -dL/dI_last = (g - n (n.g)) / s,  n.g = (1 - c/s) / L,
-// is formed inside the blend adjoint from (s, c, L) without another pass.
+// is formed inside the blend adjoint without another pass, from 1/s, n.g and 1/L that
+// the last block rounds to FP32 once per pair (no FP64 arithmetic per pixel).
 // Each block reduces a slice of one pair into FP64 partials; the last block of the
 // pair to finish (atomic ticket after a fence) adds the partials in a fixed order, so
 // the scalars do not depend on block scheduling.
@@ -104,10 +105,17 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
         double s = sqrt(S2t);
         double L2 = 1.0 - 2.0 * CRt / s + E2t;
         double L = sqrt(L2 > 0.0 ? L2 : 0.0);
-        ws.loss_scal[4 * pi + 0] = s;
-        ws.loss_scal[4 * pi + 1] = CRt;
-        ws.loss_scal[4 * pi + 2] = E2t;
-        ws.loss_scal[4 * pi + 3] = L;
+        LossScal &sc = ws.loss_scal[pi];
+        sc.s = s;
+        sc.cross = CRt;
+        sc.e2 = E2t;
+        sc.L = L;
+        // factors of the per-pixel image gradient, rounded once here so the adjoint
+        // blend's per-pixel prologue stays in FP32
+        sc.inv_s = (float)(1.0 / s);
+        sc.ndotg = (float)((1.0 - CRt / s) / L);
+        sc.inv_L = (float)(1.0 / L);
+        sc.pad = 0.0f;
         if (loss_out) loss_out[pi] = L;
         if (!(L == L) || !(s > 0.0)) atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
         ws.loss_done[pi] = 0u;

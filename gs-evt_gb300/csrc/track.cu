@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
             finite &= isfinite(grad[i]);
         }
         for (int p = 0; p < num_pairs; ++p)
-            if (pairs[p].pose == pi) S.loss = loss ? loss[p] : ws.loss_scal[4 * p + 3];
+            if (pairs[p].pose == pi) S.loss = loss ? loss[p] : ws.loss_scal[p].L;
         s_ok = finite;
         if (!finite) atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
         // stage control: the velocity learning-rate ramp of the fine stage

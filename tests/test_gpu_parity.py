@@ -185,6 +185,25 @@ def _pair_frame(m, cam, R, t, lin, ang, dtau, E, unsigned=False):
     return fr, ((Rl, tl), (Rn, tn))
 
 
+@pytest.mark.parametrize("size", [(320, 240, 300.0, 20000), (640, 480, 500.0, 60000)])
+def test_alpha_support_rectangles_keep_images_bit_exact(size):
+    """Frames with tracking pairs bin each Gaussian only into the tiles its alpha support
+    (o * exp(-q/2) >= 1/255) can reach; frames without pairs use the 3-sigma rectangles.
+    The same two views rendered both ways give bit-identical images with fewer pairs."""
+    W, H, f, n = size
+    m, cam, R, t, lin, ang, dtau, E = _pair_setup(n=n, W=W, H=H, f=f, seed=3, pose_seed=70)
+    fr, views = _pair_frame(m, cam, R, t, lin, ang, dtau, E)
+    fr.render(exact_keys=True)
+    s, keep = _map_spec(m, True)
+    plain = GSFrame([s], [_view(Rv, tv, cam, 0) for (Rv, tv) in views], channels=1, device=DEV)
+    plain.render(exact_keys=True)
+    torch.cuda.synchronize()
+    assert fr.status()[0] == 0 and plain.status()[0] == 0
+    assert 0 < fr.num_keys < plain.num_keys
+    for i in range(2):
+        assert torch.equal(fr.pixels(i), plain.pixels(i)), i
+
+
 @pytest.mark.parametrize("unsigned", [False, True])
 def test_pair_loss_and_twist_gradients(unsigned):
     m, cam, R, t, lin, ang, dtau, E = _pair_setup(unsigned=unsigned)
