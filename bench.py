@@ -557,13 +557,14 @@ def main():
             traffic = json.load(open(tpath)).get(args.workload, {}).get(top)
         except Exception:
             traffic = None
-    # kernels per iteration of the batched step: preprocess, scan, compaction, depth sort
-    # (histogram, 4 passes), sorted sums, paired scan, coarse duplication, super-tile sort
-    # (histogram, passes), super-tile ranges, tile filter, blend fwd, loss, blend bwd,
-    # preprocess bwd, finalize
+    # kernels per iteration of the batched step: preprocess, visible scan, compaction, 4
+    # depth-sort passes, sorted sums, paired scan, coarse duplication, super-tile sort
+    # passes (+ a super-tile range kernel when there are two), tile filter, blend fwd,
+    # loss, blend bwd, preprocess bwd, finalize
     L = bt.frame.L
-    super_bits = max(1, int(L.total_tiles // 4 + L.num_views).bit_length())
-    launches_per_iter = 19 + (super_bits + 7) // 8
+    nsup = L.super_tiles if L.super_tiles > 0 else L.total_tiles // 4 + L.num_views + 1
+    super_passes = (max(1, int(nsup - 1).bit_length()) + 7) // 8
+    launches_per_iter = 16 + super_passes + (1 if super_passes > 1 else 0)
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -578,7 +579,11 @@ def main():
                                                 "batched_over_plain": (1000.0 / ms) / (1000.0 / plain_ms)},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes": algo[top], "stage_ms": stages},
+                     "algorithmic_bytes": algo[top], "stage_ms": stages,
+                     "stage_path": "stages run one at a time through the frame API: bin_and_sort is the full "
+                                   "tile sort and preprocess_bwd the uncached twist adjoint; the graphed step "
+                                   "bins through super-tiles and runs the cached adjoint (its per-kernel times "
+                                   "are in the ncu launch list)"},
         "counts": algo["counts"], "status": st,
         "gpu_launches": launches_per_iter * args.steps,
         "clocks": clk,

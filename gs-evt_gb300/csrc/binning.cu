@@ -21,11 +21,14 @@
 // (4.6x fewer pairs), a stable sort by super-tile keeps each group in depth order, and
 // k_filter_tiles cuts every tile's list out of its super-tile's group, in order.  The
 // per-tile lists equal those of steps 4-5 (gs_launch_bin_coarse).
+// With at most 256 super-tiles (the layout's super_tiles) the super-tile sort is a single
+// pass whose first block also writes the super-tile ranges (no range kernel).
 #include "common.cuh"
 
 template <typename KT>
 int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
-                     int bits, uint32_t max_keys, int kpt, const Workspace &ws, int *out_buf, cudaStream_t s);
+                     int bits, uint32_t max_keys, int kpt, const Workspace &ws, int *out_buf, cudaStream_t s,
+                     uint2 *ranges, uint32_t nranges);
 
 namespace {
 
@@ -40,12 +43,14 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t *sums, uint
     scan_blocks(sums, offs, n, total, status, capacity, part);
 }
 
-// two independent scans in one launch (the fine and the coarse pair counts)
+// Two independent scans in one launch (the fine and the coarse pair counts); also
+// resets the fine-list region cursor (status[7]) of the filter that follows.
 __global__ void __launch_bounds__(1024) k_scan_blocks2(const uint32_t *sums, uint32_t *offs, uint32_t *total,
                                                        const uint32_t *sums2, uint32_t *offs2, uint32_t *total2,
                                                        int n, uint32_t *status, uint32_t capacity)
 {
     __shared__ unsigned long long part[1024];
+    if (threadIdx.x == 0) status[7] = 0u;
     scan_blocks(sums, offs, n, total, status, capacity, part);
     __syncthreads();
     scan_blocks(sums2, offs2, n, total2, status, capacity, part);
@@ -123,6 +128,7 @@ struct BinParams {
     Workspace ws;
     uint32_t capacity;
     int rgb;
+    uint32_t super_bound;  // number of super-tile ids the layout provides for
 };
 
 __global__ void __launch_bounds__(GS_BLOCK) k_compact(BinParams p)
@@ -212,7 +218,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sorted_sums(BinParams p, const uin
             carry += wsum2[0];
             __syncthreads();
         }
-        if (threadIdx.x == 0) p.ws.soffs[p.num_views] = carry;
+        if (threadIdx.x == 0) {
+            p.ws.soffs[p.num_views] = carry;
+            // more super-tiles than the layout provides ids for: k_duplicate_coarse clamps
+            // the ids (results are wrong but every access stays in bounds)
+            if (carry > p.super_bound) atomicOr(p.ws.status, GSEVT_STATUS_LAYOUT);
+        }
     }
 }
 
@@ -331,7 +342,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_duplicate_coarse(BinParams p, cons
         const uint32_t idx = wbase + k;
         if (k < wtotal && idx < p.capacity) {
             const int y = ssy0 + (int)(q / (uint32_t)ssrw), x = ssx0 + (int)(q % (uint32_t)ssrw);
-            p.ws.keys[0][idx] = (uint32_t)(ssoff + y * sstx + x);
+            // ids past the layout's count (flagged by k_sorted_sums) are clamped in range
+            p.ws.keys[0][idx] = min((uint32_t)(ssoff + y * sstx + x), p.super_bound - 1u);
             p.ws.vals[0][idx] = svg;
         }
     }
@@ -499,6 +511,7 @@ BinParams make_params(const gsevt_frame *f, const Workspace &ws)
     p.ws = ws;
     p.capacity = f->L.key_capacity;
     p.rgb = f->L.channels == 3;
+    p.super_bound = gs_super_bound(f->L);
     return p;
 }
 
@@ -525,7 +538,7 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
     uint32_t *dk[2] = {ws.dkeys[0], ws.dkeys[1]};
     uint32_t *dv[2] = {ws.dvals[0], ws.dvals[1]};
     int st = gs_launch_sort_t<uint32_t>(dk, dv, ws.status + 5, (uint32_t)L.num_vg, 32, (uint32_t)L.num_vg,
-                                       GS_SORT_KPT_DEPTH, ws, &buf, s);
+                                       GS_SORT_KPT_DEPTH, ws, &buf, s, nullptr, 0);
     if (st) return st;
     if (buf != 0) return GSEVT_ERR_ARG;  // 4 passes: the result is back in buffer 0
     if (coarse) {
@@ -554,7 +567,7 @@ int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, 
     uint32_t *k[2] = {ws.keys[0], ws.keys[1]};
     uint32_t *v[2] = {ws.vals[0], ws.vals[1]};
     int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 1, L.key_capacity, gs_tile_bits(L), max_keys,
-                                       GS_SORT_KPT_TILES, ws, &buf, s);
+                                       GS_SORT_KPT_TILES, ws, &buf, s, nullptr, 0);
     if (st) return st;
     if (buf != gs_tile_sort_buffer(L)) return GSEVT_ERR_ARG;
     int blocks = (int)std::min<uint32_t>((max_keys + 255) / 256, 152u * 16u);
@@ -564,7 +577,7 @@ int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, 
 }
 
 // Batched-tracker binning through 4x4-tile super-tiles (after gs_launch_depth_order with
-// coarse = true): coarse duplication in depth order, stable sort of the coarse pairs by
+// coarse = true, which also resets the fine-list region cursor): coarse duplication in depth order, stable sort of the coarse pairs by
 // super-tile, super-tile ranges, and the per-super-tile filter that writes the fine
 // lists and the tile ranges.  The fine lists and ranges equal those of
 // gs_launch_bin (depth order within a tile, ties in slot order); only the values are
@@ -575,25 +588,28 @@ int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max
     const gsevt_layout &L = f->L;
     *fine_vals = ws.vals[0];
     const uint32_t nsup = gs_super_bound(L);
-    cudaMemsetAsync(ws.sranges, 0, (size_t)nsup * 8, s);
-    cudaMemsetAsync(ws.status + 7, 0, 4, s);  // fine-list region cursor
-    GS_CUDA_CHECK();
+    const int bits = gs_super_bits(L);
+    // up to 256 super-tiles the sort is one pass and writes the super-tile ranges itself
+    const bool one_pass = bits <= 8;
     if (L.num_vg <= 0 || max_keys == 0 || L.total_tiles <= 0) {
         cudaMemsetAsync(ws.ranges, 0, (size_t)L.total_tiles * sizeof(uint2), s);
         GS_CUDA_CHECK();
         return GSEVT_OK;
     }
     BinParams p = make_params(f, ws);
+    if (!one_pass) cudaMemsetAsync(ws.sranges, 0, (size_t)nsup * 8, s);
     k_duplicate_coarse<<<gs_sorted_blocks(L), GS_BLOCK, 0, s>>>(p, ws.dvals[0]);
     GS_CUDA_CHECK();
     int buf = 0;
     uint32_t *k[2] = {ws.keys[0], ws.keys[1]};
     uint32_t *v[2] = {ws.vals[0], ws.vals[1]};
-    int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 6, L.key_capacity, gs_super_bits(L), max_keys,
-                                        GS_SORT_KPT_TILES, ws, &buf, s);
+    int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 6, L.key_capacity, bits, max_keys, GS_SORT_KPT_TILES, ws,
+                                        &buf, s, one_pass ? ws.sranges : nullptr, one_pass ? nsup : 0u);
     if (st) return st;
-    int blocks = (int)std::min<uint32_t>((max_keys + 255) / 256, 152u * 16u);
-    k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status + 6, L.key_capacity, ws.sranges);
+    if (!one_pass) {
+        int blocks = (int)std::min<uint32_t>((max_keys + 255) / 256, 152u * 16u);
+        k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status + 6, L.key_capacity, ws.sranges);
+    }
     k_filter_tiles<<<nsup, FILTER_WARPS * 32, 0, s>>>(f->views, L.num_views, ws, ws.vals[buf], ws.vals[buf ^ 1],
                                                      L.key_capacity);
     GS_CUDA_CHECK();

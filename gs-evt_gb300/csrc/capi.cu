@@ -59,6 +59,9 @@ extern "C" int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream)
     cudaMemsetAsync(ws.status, 0, 64, s);
     cudaMemsetAsync(ws.sort_lookback, 0, (size_t)gs_lookback_tiles(f->L) * 256 * 8, s);
     if (f->L.num_pairs > 0) cudaMemsetAsync(ws.loss_done, 0, (size_t)f->L.num_pairs * 4, s);
+    // tile ranges always point inside the value buffers, even for a tile that a step
+    // whose layout check failed (GSEVT_STATUS_LAYOUT) leaves unwritten
+    cudaMemsetAsync(ws.ranges, 0, (size_t)f->L.total_tiles * sizeof(uint2), s);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

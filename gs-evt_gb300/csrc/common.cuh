@@ -117,9 +117,11 @@ inline uint32_t gs_lookback_tiles(const gsevt_layout &L)
     return std::max(gs_sort_tiles(cap, GS_SORT_KPT_TILES), gs_sort_tiles(vg, GS_SORT_KPT_DEPTH));
 }
 inline int gs_tile_bits(const gsevt_layout &L) { return L.sort_bits - 32; }
-// upper bound on the number of super-tiles: ceil(tx/4) ceil(ty/4) <= floor(tx ty / 4) + 1 per view
+// number of super-tile ids: the layout's exact count, else an upper bound
+// (ceil(tx/4) ceil(ty/4) <= floor(tx ty / 4) + 1 per view)
 inline uint32_t gs_super_bound(const gsevt_layout &L)
 {
+    if (L.super_tiles > 0) return (uint32_t)L.super_tiles;
     return (uint32_t)(L.total_tiles > 0 ? L.total_tiles : 0) / 4 + (uint32_t)(L.num_views > 0 ? L.num_views : 0) + 1;
 }
 inline int gs_super_bits(const gsevt_layout &L)
@@ -129,6 +131,15 @@ inline int gs_super_bits(const gsevt_layout &L)
     return (int)b;
 }
 inline int gs_tile_sort_buffer(const gsevt_layout &L) { return ((gs_tile_bits(L) + 7) / 8) & 1; }
+
+// Reserves the look-back epochs of a sort's passes: status[4] = first epoch of this sort,
+// status[2] = last epoch used so far.  One thread, before any pass of the sort runs.
+__device__ __forceinline__ void gs_sort_reserve_epochs(uint32_t *status, int passes)
+{
+    const uint32_t e = status[2];
+    status[4] = e + 1;
+    status[2] = e + (uint32_t)passes;
+}
 
 // Carves the workspace in a fixed order; with base == nullptr it only sizes it.
 inline Workspace gs_carve(const gsevt_layout &L, void *base)

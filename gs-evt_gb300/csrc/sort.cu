@@ -29,12 +29,7 @@ __global__ void k_sort_hist(const KT *keys, const uint32_t *count, uint32_t capa
                             uint32_t *status)
 {
     __shared__ uint32_t sh[GS_MAX_PASSES][256];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        // epochs of this sort's passes: status[2] last epoch used, status[4] first epoch
-        const uint32_t e = status[2];
-        status[4] = e + 1;
-        status[2] = e + (uint32_t)passes;
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) gs_sort_reserve_epochs(status, passes);
     for (int i = threadIdx.x; i < GS_MAX_PASSES * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     uint32_t K = min(*count, capacity);
@@ -63,6 +58,8 @@ struct PassParams {
     const uint32_t *count;      // number of keys (device word)
     uint32_t capacity;
     int pass;
+    uint2 *ranges;              // single-pass sorts: [start, end) of keys 0..nranges-1, or null
+    uint32_t nranges;
 };
 
 template <typename KT, int SORT_KPT>
@@ -80,6 +77,23 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t K = min(*p.count, p.capacity);
     const uint32_t ntiles = (K + SORT_TILE - 1) / SORT_TILE;
+    if (p.ranges && blockIdx.x == 0) {
+        // a single-pass sort's digit is the whole key: key d occupies bucket d of the
+        // output, [exclusive prefix of the histogram, + its count)
+        const uint32_t c = p.hist[tid];
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wscan[w] = inc;
+        __syncthreads();
+        uint32_t wb = 0;
+        for (int i = 0; i < w; ++i) wb += wscan[i];
+        if ((uint32_t)tid < p.nranges) p.ranges[tid] = make_uint2(wb + inc - c, wb + inc);
+        __syncthreads();
+    }
     // A pass whose digit is the same for every key is the identity permutation of a
     // stable sort: copy keys and values, with no ranking or look-back.
     if (__syncthreads_or(p.hist[tid] == K)) {
@@ -220,14 +234,18 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
 // result is in buffer index (passes & 1), returned through *out_buf.  max_keys bounds
 // the grid (a host-known count, or the capacity when the count is only known on the
 // device).  The look-back table must hold gs_sort_tiles(capacity, kpt) * 256 entries.
+// ranges: for a single-pass sort (bits <= 8), also write the [start, end) range of
+// every key below nranges (no separate range pass); null otherwise.
 template <typename KT>
 int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
-                     int bits, uint32_t max_keys, int kpt, const Workspace &ws, int *out_buf, cudaStream_t s)
+                     int bits, uint32_t max_keys, int kpt, const Workspace &ws, int *out_buf, cudaStream_t s,
+                     uint2 *ranges, uint32_t nranges)
 {
     if (kpt != 4 && kpt != 8 && kpt != 12) return GSEVT_ERR_ARG;
     int passes = (bits + 7) / 8;
     if (passes < 1) passes = 1;
     if (passes > GS_MAX_PASSES || passes * 8 > (int)(8 * sizeof(KT)) + 7) return GSEVT_ERR_ARG;
+    if (ranges && (passes != 1 || nranges > 256)) return GSEVT_ERR_ARG;
     *out_buf = passes & 1;
     if (max_keys > capacity) max_keys = capacity;
     if (max_keys == 0) return GSEVT_OK;
@@ -254,6 +272,8 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
         p.count = count;
         p.capacity = capacity;
         p.pass = pass;
+        p.ranges = ranges;
+        p.nranges = nranges;
         if (kpt == 4) k_sort_pass<KT, 4><<<tiles, GS_BLOCK, 0, s>>>(p);
         else if (kpt == 8) k_sort_pass<KT, 8><<<tiles, GS_BLOCK, 0, s>>>(p);
         else k_sort_pass<KT, 12><<<tiles, GS_BLOCK, 0, s>>>(p);
@@ -264,4 +284,5 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
 
 template int gs_launch_sort_t<uint32_t>(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_t *count,
                                         uint32_t capacity, int bits, uint32_t max_keys, int kpt,
-                                        const Workspace &ws, int *out_buf, cudaStream_t s);
+                                        const Workspace &ws, int *out_buf, cudaStream_t s, uint2 *ranges,
+                                        uint32_t nranges);

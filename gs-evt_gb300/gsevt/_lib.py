@@ -22,6 +22,7 @@ ERRORS = {
 STATUS_KEY_OVERFLOW = 1
 STATUS_SORT_TIMEOUT = 2
 STATUS_NONFINITE = 4
+STATUS_LAYOUT = 8
 TILE = 16
 MAP_PLANES = 15
 LOSS_PIXELS_PER_BLOCK = 2048
@@ -68,7 +69,7 @@ class Layout(C.Structure):
                 ("num_vg", C.c_int32), ("num_scan_blocks", C.c_int32),
                 ("preprocess_blocks", C.c_int32), ("total_tiles", C.c_int32),
                 ("total_pixels", C.c_int32), ("channels", C.c_int32), ("sort_bits", C.c_int32),
-                ("key_capacity", C.c_uint32), ("loss_blocks", C.c_int32)]
+                ("key_capacity", C.c_uint32), ("loss_blocks", C.c_int32), ("super_tiles", C.c_int32)]
 
 
 class Frame(C.Structure):

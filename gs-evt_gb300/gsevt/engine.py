@@ -94,10 +94,11 @@ class GSFrame:
         L = _lib.Layout()
         L.num_views, L.num_maps, L.num_pairs = len(views), len(maps), len(self.pairs)
         self.vg_offset, self.sb_offset, self.tile_offset, self.pix_offset = [], [], [], []
-        vg = sb = tiles = pix = 0
+        vg = sb = tiles = pix = supers = 0
         for v in views:
             n = maps[v.map_index].n
             tx, ty = (v.width + 15) // 16, (v.height + 15) // 16
+            supers += ((tx + 3) // 4) * ((ty + 3) // 4)
             self.vg_offset.append(vg); self.sb_offset.append(sb)
             self.tile_offset.append(tiles); self.pix_offset.append(pix)
             vg += n
@@ -105,6 +106,7 @@ class GSFrame:
             tiles += tx * ty
             pix += v.width * v.height
         L.num_vg, L.num_scan_blocks, L.total_tiles, L.total_pixels = vg, sb, tiles, pix
+        L.super_tiles = supers
         self.block_offset = []
         pb = 0
         for m in maps:

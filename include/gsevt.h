@@ -47,6 +47,7 @@ enum {
 #define GSEVT_STATUS_KEY_OVERFLOW 1u
 #define GSEVT_STATUS_SORT_TIMEOUT 2u
 #define GSEVT_STATUS_NONFINITE 4u
+#define GSEVT_STATUS_LAYOUT 8u /* the views need more super-tiles than layout.super_tiles */
 
 #define GSEVT_TILE 16
 #define GSEVT_LOSS_PIXELS_PER_BLOCK 2048 /* pixels reduced by one loss block */
@@ -133,6 +134,10 @@ typedef struct gsevt_layout {
     int32_t sort_bits;          /* 32 + bits of (total_tiles - 1) */
     uint32_t key_capacity;      /* max (tile, Gaussian) pairs */
     int32_t loss_blocks;        /* sum over pairs of loss-reduction blocks */
+    int32_t super_tiles;        /* sum over views of ceil(tiles_x / 4) * ceil(tiles_y / 4)
+                                 * (the batched step's 4x4-tile super-tiles); 0: use the
+                                 * bound total_tiles / 4 + num_views + 1, which can cost the
+                                 * super-tile sort a second pass */
 } gsevt_layout;
 
 /* One rendering frame: layout, device tables, workspace and caller-owned outputs. */
@@ -155,7 +160,7 @@ typedef struct gsevt_frame {
 /* ---- sizing ---- */
 size_t gsevt_workspace_bytes(const gsevt_layout *L);
 /* Zero the parts of a fresh workspace that must start at zero (status words, sort
- * look-back table, loss tickets).  Call once after allocating it. */
+ * look-back table, loss tickets, tile ranges).  Call once after allocating it. */
 int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream);
 /* sizeof of the ABI structs, for binding checks: view, map, map_grads, pair, layout,
  * frame, pose_state (7 entries).  Touches no GPU state. */

@@ -103,7 +103,9 @@ def test_super_tile_lists_match_tile_sort(sizes):
     st, _ = fr.status()
     assert st == 0, st
     # the super-tile sort ends in buffer (passes & 1); the fine lists are in the other one
-    bound = L.total_tiles // 4 + L.num_views + 1
+    # (one pass for the 32 super-tiles of the small pair, two for the 320 of the large one)
+    bound = L.super_tiles
+    assert bound == sum(((v.width + 63) // 64) * ((v.height + 63) // 64) for v in fr.views)
     bits = max(1, int(bound - 1).bit_length())
     fine_buf = (((bits + 7) // 8) & 1) ^ 1
     T = L.total_tiles
@@ -147,6 +149,32 @@ def test_super_tile_overflow_is_reported_not_faulting():
     T = bt.frame.L.total_tiles
     rng = _ws_region(bt.frame, "ranges", torch.int32, 2 * T).view(T, 2).cpu().numpy()
     assert (rng[:, 1] >= rng[:, 0]).all() and rng.max() <= 1000
+
+
+def test_layout_with_too_few_super_tiles_is_reported_not_faulting():
+    """A layout whose super_tiles is below the views' super-tile count: the step flags
+    GSEVT_STATUS_LAYOUT, every access stays in bounds (ids clamped, tile ranges inside the
+    buffers) and the GPU stays usable for a correct step afterwards."""
+    s0, pk0, sig0, _, _ = _scenario(20000, 320, 240, 300.0, 5, 30000)
+    R, t = synthetic.perturb(s0.gt_R, s0.gt_t, np.random.default_rng(8), 0.05, 3.0)
+    c = s0.camera
+    prob = Problem(0, R, t, s0.init_lin, s0.init_ang, s0.delta_tau, c.width, c.height, c.fx, c.fy,
+                   sig0[0].reshape(-1), opt_vel=True)
+    maps = [{"packed": pk0, "n": 20000}]
+    bt = BatchedTracker(maps, [prob], device=DEV)
+    assert bt.frame._frame.L.super_tiles == 40
+    bt.frame._frame.L.super_tiles = 3  # the workspace was sized for 40; fewer ids only shrink regions
+    bt.step()
+    torch.cuda.synchronize()
+    st, _ = bt.frame.status()
+    assert st & _lib.STATUS_LAYOUT
+    T = bt.frame.L.total_tiles
+    rng = _ws_region(bt.frame, "ranges", torch.int32, 2 * T).view(T, 2).cpu().numpy()
+    assert (rng[:, 1] >= rng[:, 0]).all() and rng.max() <= bt.frame.L.key_capacity
+    good = BatchedTracker(maps, [prob], device=DEV)
+    good.step()
+    torch.cuda.synchronize()
+    assert good.frame.status()[0] == 0
 
 
 def test_batched_step_with_a_problem_that_sees_nothing():
