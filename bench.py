@@ -14,6 +14,9 @@ and the pose / velocity update (utils/tracker.py:176-222).
   plain      the plain per-view drop-in path (reference-structured tracker over the
              drop-in GaussianRasterizer, torch glue and torch Adam), timed beside it
   roofline   dominant stage of the iteration against the measured HBM bandwidth
+  iteration_roofline  canonical compulsory bytes of a whole iteration (attribute reads,
+             projected records, pairs, pixels; counts from the reference's 3-sigma
+             binning) times iterations/s, against the same peak
   cpu_baseline  the CPU oracle (C + OpenMP) running the same iteration on the host
              cores, on a bounded sample
 
@@ -290,6 +293,37 @@ def algorithmic_bytes(bt, prob):
     }
 
 
+def iteration_bytes(prob, device):
+    """Canonical compulsory bytes of one tracking iteration (the same formula for the plain
+    and the batched path): 236 N M + 236 U + sum over views of (8 N + 88 N_v + 108 K_v +
+    24 P_v) + 20 P per pair, with N_v, K_v and U from the reference's 3-sigma binning of
+    the two views at the starting pose (a frame without render pairs bins that way)."""
+    import torch
+    from gsevt import _lib
+    from gsevt import pose as gpose
+    from gsevt.engine import GSFrame, MapSpec, ViewSpec
+    sc = prob["scenario"]
+    cam = sc.camera
+    views = []
+    for T in gpose.pair_poses(sc.init_R, sc.init_t, sc.init_lin, sc.init_ang, sc.delta_tau):
+        R, t = T[:3, :3], T[:3, 3]
+        views.append(ViewSpec(prob["W"], prob["H"], 0, R=R, t=t, P=cam.proj, campos=gpose.campos(R, t),
+                              tanfovx=cam.tanfovx, tanfovy=cam.tanfovy))
+    n = prob["n"]
+    fr = GSFrame([MapSpec(n, packed=prob["packed"])], views, channels=1, device=device)
+    fr.render(exact_keys=True)
+    off = _lib.workspace_offsets(fr.L)["bin"]
+    touched = fr.workspace[off:off + 16 * fr.L.num_vg].view(torch.int32).view(-1, 4)[:, 0].view(len(views), n)
+    vis = touched > 0
+    nv = int(vis.sum().item())
+    u = int(vis.any(dim=0).sum().item())
+    K = int(fr.num_keys)
+    P = fr.L.total_pixels
+    b = 236 * n + 236 * u + 8 * n * len(views) + 88 * nv + 108 * K + 24 * P + 20 * (P // 2)
+    return {"bytes_per_iter": b, "gaussians": n, "visible_any_view": u, "visible_slots": nv, "keys_3sigma": K,
+            "pixels": P}
+
+
 def time_batched(bt, steps, warmup, flush):
     import torch
     bt.capture(warmup=max(1, warmup))
@@ -557,14 +591,16 @@ def main():
             traffic = json.load(open(tpath)).get(args.workload, {}).get(top)
         except Exception:
             traffic = None
-    # kernels per iteration of the batched step: preprocess, visible scan, compaction, 4
-    # depth-sort passes, sorted sums, paired scan, coarse duplication, super-tile sort
-    # passes (+ a super-tile range kernel when there are two), tile filter, blend fwd,
-    # loss, blend bwd, preprocess bwd, finalize
+    # kernels per iteration of the batched step: preprocess, visible scan, compaction,
+    # depth sort (histogram, 4 passes), sorted sums, paired scan, coarse duplication,
+    # super-tile sort (histogram, passes, + a super-tile range kernel when there are two),
+    # tile filter, blend fwd, loss, blend bwd, preprocess bwd, finalize
     L = bt.frame.L
     nsup = L.super_tiles if L.super_tiles > 0 else L.total_tiles // 4 + L.num_views + 1
     super_passes = (max(1, int(nsup - 1).bit_length()) + 7) // 8
-    launches_per_iter = 16 + super_passes + (1 if super_passes > 1 else 0)
+    launches_per_iter = 18 + super_passes + (1 if super_passes > 1 else 0)
+    it_bytes = iteration_bytes(prob, dev)
+    it_gbs = it_bytes["bytes_per_iter"] * (1000.0 / ms) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -584,6 +620,9 @@ def main():
                                    "tile sort and preprocess_bwd the uncached twist adjoint; the graphed step "
                                    "bins through super-tiles and runs the cached adjoint (its per-kernel times "
                                    "are in the ncu launch list)"},
+        "iteration_roofline": dict(it_bytes, achieved=it_gbs, peak=hbm, unit="GB/s", frac=it_gbs / hbm,
+                                   note="canonical compulsory bytes of a whole iteration times the "
+                                        "batched iterations/s of one GPU, against that GPU's HBM peak"),
         "counts": algo["counts"], "status": st,
         "gpu_launches": launches_per_iter * args.steps,
         "clocks": clk,

@@ -9,8 +9,9 @@
 // __syncthreads_count says every pixel has stopped.
 //
 // Blending (the published 3DGS rule): alpha = min(0.99, o * exp(power)), skipped when
-// power > 0 or alpha < 1/255; C += c alpha T; T *= 1 - alpha.  exp is gs_expf, so the
-// per-pixel decisions and sums are bit-identical to the CPU oracle.
+// power > 0 or alpha < 1/255; C += c alpha T (one fused multiply-add); T *= 1 - alpha.
+// power is gs_power and exp is gs_expf, so the per-pixel decisions and sums are
+// bit-identical to the CPU oracle, which uses the same operation order.
 //
 // Adjoint: the same front-to-back traversal with the same decisions (no per-pixel
 // contributor lists are stored); with P_i the running prefix of c alpha T up to and
@@ -64,9 +65,9 @@ template <bool RGB> struct Batch {
 
 // Conservative pixel box of a Gaussian's alpha support.  A pixel blends the Gaussian
 // only if alpha = min(0.99, o exp(power)) >= 1/255, i.e. -power <= tau = ln(255 o).  With
-// M the conic, -power = d^T M d / 2 in exact arithmetic; the FP32 evaluation of the six
-// products and sums deviates by less than 1e-6 tr(M) |d|^2, so every pixel that can pass
-// satisfies Q(d) = d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the slack also covers
+// M the conic, -power = d^T M d / 2 in exact arithmetic; the FP32 evaluation (gs_power:
+// five products and two fused multiply-adds) deviates by less than 1e-6 tr(M) |d|^2, so
+// every pixel that can pass satisfies Q(d) = d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the slack also covers
 // gs_expf's 2 ulp and logf).  The box of that ellipse, widened by 0.1 % + 0.5 px,
 // therefore never excludes a pixel whose per-pixel test would pass, so culling against it
 // leaves every blending decision - and the result bits - unchanged.
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
                 if (done) continue;
                 const float4 A = cur.A[j], B = cur.B[j];
                 const float dx = A.x - pxf, dy = A.y - pyf;
-                const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
+                const float power = gs_power(B.x, B.y, B.z, dx, dy);
                 // power > 0, or below the Gaussian's alpha threshold (fails the alpha test anyway)
                 if (power > 0.0f || power < (EXTRAS ? cur.ell[j].w : A.z)) continue;
                 const float alpha = fminf(0.99f, B.w * gs_expf(power));
@@ -223,15 +224,15 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
                 if (test_T < 0.0001f) { done = true; continue; }
                 if (RGB) {
                     const float4 Cc = cur.C[j];
-                    C0 = C0 + (Cc.x * alpha) * T;
-                    C1 = C1 + (Cc.y * alpha) * T;
-                    C2 = C2 + (Cc.z * alpha) * T;
+                    C0 = fmaf(Cc.x * alpha, T, C0);
+                    C1 = fmaf(Cc.y * alpha, T, C1);
+                    C2 = fmaf(Cc.z * alpha, T, C2);
                 } else {
-                    C0 = C0 + (A.w * alpha) * T;
+                    C0 = fmaf(A.w * alpha, T, C0);
                 }
                 if (EXTRAS) {
-                    D = D + (A.z * alpha) * T;
-                    Aacc = Aacc + alpha * T;
+                    D = fmaf(A.z * alpha, T, D);
+                    Aacc = fmaf(alpha, T, Aacc);
                     if (p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
                     last = r * GS_BLOCK + j + 1;
                 }
@@ -406,7 +407,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                 if (!done) {
                     const float4 A = cur.A[j], B = cur.B[j];
                     const float dx = A.x - pxf, dy = A.y - pyf;
-                    const float power = -0.5f * ((B.x * dx) * dx + (B.z * dy) * dy) - (B.y * dx) * dy;
+                    const float power = gs_power(B.x, B.y, B.z, dx, dy);
                     if (power <= 0.0f && !(power < (MODE != 0 ? cur.ell[j].w : A.z))) {
                         const float G = gs_expf(power);
                         const float araw = B.w * G;

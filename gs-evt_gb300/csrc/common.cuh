@@ -54,6 +54,15 @@ __host__ __device__ __forceinline__ float gs_expf(float x)
     return p * sc;
 }
 
+// Exponent of a Gaussian at pixel offset d = mean - pixel, -(cx dx^2 + cz dy^2) / 2 - cy dx dy
+// for the conic (cx, cy, cz), in a fixed FP32 operation order (the CPU oracle's blend uses
+// the same one): the two squares are summed with one fused multiply-add.
+__host__ __device__ __forceinline__ float gs_power(float cx, float cy, float cz, float dx, float dy)
+{
+    const float q = fmaf(cz * dy, dy, (cx * dx) * dx);
+    return fmaf(-0.5f, q, -((cy * dx) * dy));
+}
+
 // ------------------------------------------------------------ workspace ---------
 // Pair loss scalars.  With d = I_next - I_last, s = |d|, n = d / s and e the event
 // frame: cross = d . e (|d| . |e| in unsigned mode), e2 = e . e, L = |n - e|.  The

@@ -247,7 +247,10 @@ void or_blend_fwd(int W, int H, int nch, const uint32_t *ranges, const uint32_t 
                     uint32_t g = vals[j];
                     float dx = mean2d[2 * g] - pxf, dy = mean2d[2 * g + 1] - pyf;
                     float cx = conic[3 * g], cy = conic[3 * g + 1], cz = conic[3 * g + 2];
-                    float power = -0.5f * ((cx * dx) * dx + (cz * dy) * dy) - (cy * dx) * dy;
+                    /* the two squares summed with one fused multiply-add (the CUDA blend's
+                     * gs_power uses the same order) */
+                    float q = fmaf(cz * dy, dy, (cx * dx) * dx);
+                    float power = fmaf(-0.5f, q, -((cy * dx) * dy));
                     if (power > 0.0f) continue;
                     float G = or_expf(power);
                     float araw = opac[g] * G;
@@ -256,9 +259,9 @@ void or_blend_fwd(int W, int H, int nch, const uint32_t *ranges, const uint32_t 
                     float test_T = T * (1.0f - alpha);
                     if (test_T < 0.0001f) break;
                     for (int ch = 0; ch < nch; ++ch)
-                        C[ch] = C[ch] + (colors[nch * g + ch] * alpha) * T;
-                    if (depth) D = D + (depth[g] * alpha) * T;
-                    A = A + alpha * T;
+                        C[ch] = fmaf(colors[nch * g + ch] * alpha, T, C[ch]);
+                    if (depth) D = fmaf(depth[g] * alpha, T, D);
+                    A = fmaf(alpha, T, A);
                     if (n_touched && test_T > 0.5f) {
 #pragma omp atomic
                         n_touched[g] += 1;
