@@ -212,31 +212,36 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
                 if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
                 const int j = c0 + __ffs(mask) - 1;
                 mask &= mask - 1;
-                if (done) continue;
+                // Every lane evaluates the candidate and the decisions become predicates
+                // (selects instead of divergent branches; stopped lanes change nothing).
+                // A candidate is skipped when power > 0 or below the Gaussian's alpha
+                // threshold (it fails the alpha test anyway) or alpha < 1/255; the pixel
+                // stops before a candidate that would take T below 1e-4.
                 const float4 A = cur.A[j], B = cur.B[j];
                 const float dx = A.x - pxf, dy = A.y - pyf;
                 const float power = gs_power(B.x, B.y, B.z, dx, dy);
-                // power > 0, or below the Gaussian's alpha threshold (fails the alpha test anyway)
-                if (power > 0.0f || power < (EXTRAS ? cur.ell[j].w : A.z)) continue;
                 const float alpha = fminf(0.99f, B.w * gs_expf(power));
-                if (alpha < 1.0f / 255.0f) continue;
                 const float test_T = T * (1.0f - alpha);
-                if (test_T < 0.0001f) { done = true; continue; }
+                const bool pass = !done && !(power > 0.0f) && !(power < (EXTRAS ? cur.ell[j].w : A.z)) &&
+                                  !(alpha < 1.0f / 255.0f);
+                const bool stop = pass && test_T < 0.0001f;
+                const bool use = pass && !stop;
+                done = done || stop;
                 if (RGB) {
                     const float4 Cc = cur.C[j];
-                    C0 = fmaf(Cc.x * alpha, T, C0);
-                    C1 = fmaf(Cc.y * alpha, T, C1);
-                    C2 = fmaf(Cc.z * alpha, T, C2);
+                    C0 = use ? fmaf(Cc.x * alpha, T, C0) : C0;
+                    C1 = use ? fmaf(Cc.y * alpha, T, C1) : C1;
+                    C2 = use ? fmaf(Cc.z * alpha, T, C2) : C2;
                 } else {
-                    C0 = fmaf(A.w * alpha, T, C0);
+                    C0 = use ? fmaf(A.w * alpha, T, C0) : C0;
                 }
                 if (EXTRAS) {
-                    D = fmaf(A.z * alpha, T, D);
-                    Aacc = fmaf(alpha, T, Aacc);
-                    if (p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
-                    last = r * GS_BLOCK + j + 1;
+                    D = use ? fmaf(A.z * alpha, T, D) : D;
+                    Aacc = use ? fmaf(alpha, T, Aacc) : Aacc;
+                    if (use && p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
+                    last = use ? r * GS_BLOCK + j + 1 : last;
                 }
-                T = test_T;
+                T = use ? test_T : T;
             }
         }
         __syncthreads();  // the next iteration overwrites this buffer
@@ -400,64 +405,58 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                 if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
                 const int j = c0 + __ffs(mask) - 1;
                 mask &= mask - 1;
+                // The forward's decisions as predicates (every lane evaluates the candidate;
+                // a lane that does not blend it contributes zeros and keeps its state).
+                const float4 A = cur.A[j], B = cur.B[j];
+                const float dx = A.x - pxf, dy = A.y - pyf;
+                const float power = gs_power(B.x, B.y, B.z, dx, dy);
+                const float G = gs_expf(power);
+                const float araw = B.w * G;
+                const float alpha = fminf(0.99f, araw);
+                const float test_T = T * (1.0f - alpha);
+                const bool pass = !done && !(power > 0.0f) && !(power < (MODE != 0 ? cur.ell[j].w : A.z)) &&
+                                  !(alpha < 1.0f / 255.0f);
+                const bool stop = pass && test_T < 0.0001f;
+                const bool contrib = pass && !stop;
+                done = done || stop;
                 float gv[10];
+                float col[3];
+                if (RGB) { const float4 Cc = cur.C[j]; col[0] = Cc.x; col[1] = Cc.y; col[2] = Cc.z; }
+                else { col[0] = A.w; col[1] = col[2] = 0.0f; }
+                const float wgt = contrib ? alpha * T : 0.0f;
+                // gradient-only term: the 2-ulp fast reciprocal suffices
+                const float inv1m = __fdividef(1.0f, 1.0f - alpha);
+                float dal = 0.0f;
 #pragma unroll
-                for (int k = 0; k < 10; ++k) gv[k] = 0.0f;
-                bool contrib = false;
-                if (!done) {
-                    const float4 A = cur.A[j], B = cur.B[j];
-                    const float dx = A.x - pxf, dy = A.y - pyf;
-                    const float power = gs_power(B.x, B.y, B.z, dx, dy);
-                    if (power <= 0.0f && !(power < (MODE != 0 ? cur.ell[j].w : A.z))) {
-                        const float G = gs_expf(power);
-                        const float araw = B.w * G;
-                        const float alpha = fminf(0.99f, araw);
-                        if (alpha >= 1.0f / 255.0f) {
-                            const float test_T = T * (1.0f - alpha);
-                            if (test_T < 0.0001f) {
-                                done = true;
-                            } else {
-                                contrib = true;
-                                float col[3];
-                                if (RGB) { const float4 Cc = cur.C[j]; col[0] = Cc.x; col[1] = Cc.y; col[2] = Cc.z; }
-                                else { col[0] = A.w; col[1] = col[2] = 0.0f; }
-                                const float wgt = alpha * T;
-                                // gradient-only term: the 2-ulp fast reciprocal suffices
-                                const float inv1m = __fdividef(1.0f, 1.0f - alpha);
-                                float dal = 0.0f;
-#pragma unroll
-                                for (int c = 0; c < (RGB ? 3 : 1); ++c) {
-                                    Pc[c] = __fmaf_rn(col[c], wgt, Pc[c]);
-                                    const float suffix = Cimg[c] - Pc[c];
-                                    dal = __fmaf_rn(gC[c], __fmaf_rn(-suffix, inv1m, T * col[c]), dal);
-                                }
-                                if (MODE != 0) {
-                                    PD = __fmaf_rn(A.z, wgt, PD);
-                                    PA = PA + wgt;
-                                    dal = __fmaf_rn(gD, __fmaf_rn(-(Dtot - PD), inv1m, T * A.z), dal);
-                                    dal = __fmaf_rn(gA, __fmaf_rn(-(Atot - PA), inv1m, T), dal);
-                                    gv[7] = gD * wgt;
-                                }
-                                gv[6] = gC[0] * wgt;
-                                if (RGB) { gv[8] = gC[1] * wgt; gv[9] = gC[2] * wgt; }
-                                if (araw <= 0.99f) {
-                                    // d power / d(mean, conic) is linear in the conic: accumulate
-                                    // the moments of dpow over (dx, dy) and apply the conic once per
-                                    // Gaussian when the batch is flushed
-                                    gv[5] = dal * G;
-                                    const float dpow = dal * araw;
-                                    const float mx = dpow * dx, my = dpow * dy;
-                                    gv[0] = mx;
-                                    gv[1] = my;
-                                    gv[2] = mx * dx;
-                                    gv[3] = mx * dy;
-                                    gv[4] = my * dy;
-                                }
-                                T = test_T;
-                            }
-                        }
-                    }
+                for (int c = 0; c < (RGB ? 3 : 1); ++c) {
+                    Pc[c] = contrib ? __fmaf_rn(col[c], wgt, Pc[c]) : Pc[c];
+                    const float suffix = Cimg[c] - Pc[c];
+                    dal = __fmaf_rn(gC[c], __fmaf_rn(-suffix, inv1m, T * col[c]), dal);
                 }
+                if (MODE != 0) {
+                    PD = contrib ? __fmaf_rn(A.z, wgt, PD) : PD;
+                    PA = contrib ? PA + wgt : PA;
+                    dal = __fmaf_rn(gD, __fmaf_rn(-(Dtot - PD), inv1m, T * A.z), dal);
+                    dal = __fmaf_rn(gA, __fmaf_rn(-(Atot - PA), inv1m, T), dal);
+                }
+                gv[7] = gD * wgt;
+                gv[6] = gC[0] * wgt;
+                gv[8] = gC[1] * wgt;
+                gv[9] = gC[2] * wgt;
+                // below the 0.99 clamp alpha depends on the power and the opacity
+                const float dun = (contrib && araw <= 0.99f) ? dal : 0.0f;
+                gv[5] = dun * G;
+                // d power / d(mean, conic) is linear in the conic: accumulate the moments of
+                // dpow over (dx, dy) and apply the conic once per Gaussian when the batch is
+                // flushed
+                const float dpow = dun * araw;
+                const float mx = dpow * dx, my = dpow * dy;
+                gv[0] = mx;
+                gv[1] = my;
+                gv[2] = mx * dx;
+                gv[3] = mx * dy;
+                gv[4] = my * dy;
+                T = contrib ? test_T : T;
                 if (__any_sync(0xffffffffu, contrib)) {
                     constexpr int NV = Comps<MODE>::padded;
                     constexpr int SH = NV == 8 ? 2 : 1;  // 5 - log2(NV)
