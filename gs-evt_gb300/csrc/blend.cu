@@ -103,23 +103,34 @@ __device__ __forceinline__ float4 gauss_box(float4 A, float4 B, float4 *ell)
 // 1.4e-4 Q (|b| <= 0.995 sqrt(ac) bounds a dx^2 + c dy^2 by 400 Q) plus a second-order
 // term from the rounded edge minimiser, both far below the slack of the comparison
 // (tau * 1.001 + 0.01).  So this never rejects a Gaussian a pixel of the rectangle blends.
+// Both edge minima are evaluated and selected (no divergent branches).
 __device__ __forceinline__ bool ellipse_hits(float mx, float my, float4 E, float x0, float x1, float y0, float y1)
 {
     const bool inx = mx >= x0 && mx <= x1, iny = my >= y0 && my <= y1;
-    if (inx && iny) return true;
     const float a = E.x, b = E.y, c = E.z;
-    float q = 1e30f;
-    if (!inx) {
-        const float dx = mx - (mx < x0 ? x0 : x1);
-        const float dy = fminf(fmaxf(-__fdividef(b * dx, c), my - y1), my - y0);
-        q = (a * dx) * dx + 2.0f * ((b * dx) * dy) + (c * dy) * dy;
-    }
-    if (!iny) {
-        const float dy = my - (my < y0 ? y0 : y1);
-        const float dx = fminf(fmaxf(-__fdividef(b * dy, a), mx - x1), mx - x0);
-        q = fminf(q, (a * dx) * dx + 2.0f * ((b * dx) * dy) + (c * dy) * dy);
-    }
-    return q <= -E.w * 1.001f + 0.01f;
+    // the x-facing edge
+    const float dxa = mx - (mx < x0 ? x0 : x1);
+    const float dya = fminf(fmaxf(-__fdividef(b * dxa, c), my - y1), my - y0);
+    const float qa = (a * dxa) * dxa + 2.0f * ((b * dxa) * dya) + (c * dya) * dya;
+    // the y-facing edge
+    const float dyb = my - (my < y0 ? y0 : y1);
+    const float dxb = fminf(fmaxf(-__fdividef(b * dyb, a), mx - x1), mx - x0);
+    const float qb = (a * dxb) * dxb + 2.0f * ((b * dxb) * dyb) + (c * dyb) * dyb;
+    const float q = fminf(inx ? 1e30f : qa, iny ? 1e30f : qb);
+    return (inx && iny) || q <= -E.w * 1.001f + 0.01f;
+}
+
+// Which of the batch's candidates c0 + lane reach the warp's pixel rectangle (box overlap
+// and the ellipse test, both evaluated for every lane).
+template <bool RGB>
+__device__ __forceinline__ bool warp_hit(const Batch<RGB> &cur, int c0, int n, int lane, float sx0, float sx1,
+                                         float sy0, float sy1)
+{
+    const int ci = min(c0 + lane, n - 1);
+    const float4 bx = cur.box[ci], A = cur.A[ci];
+    const bool box = bx.y >= sx0 && bx.x <= sx1 && bx.w >= sy0 && bx.z <= sy1;
+    const bool ell = ellipse_hits(A.x, A.y, cur.ell[ci], sx0, sx1, sy0, sy1);
+    return (c0 + lane < n) & box & ell;
 }
 
 // Issue the copies of batch `r` of the tile range into buffer `buf`.
@@ -198,15 +209,7 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
         bool warp_done = false;
         for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
             // candidates of this warp among the next 32 Gaussians, in depth order
-            bool hit = false;
-            if (c0 + lane < n) {
-                const float4 bx = cur.box[c0 + lane];
-                hit = bx.y >= sx0 && bx.x <= sx1 && bx.w >= sy0 && bx.z <= sy1;
-                if (hit) {
-                    const float4 A = cur.A[c0 + lane];
-                    hit = ellipse_hits(A.x, A.y, cur.ell[c0 + lane], sx0, sx1, sy0, sy1);
-                }
-            }
+            const bool hit = warp_hit(cur, c0, n, lane, sx0, sx1, sy0, sy1);
             unsigned mask = __ballot_sync(0xffffffffu, hit);
             while (mask) {
                 if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
@@ -391,15 +394,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         __syncthreads();
         bool warp_done = false;
         for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
-            bool hit = false;
-            if (c0 + lane < n) {
-                const float4 bx = cur.box[c0 + lane];
-                hit = bx.y >= sx0 && bx.x <= sx1 && bx.w >= sy0 && bx.z <= sy1;
-                if (hit) {
-                    const float4 A = cur.A[c0 + lane];
-                    hit = ellipse_hits(A.x, A.y, cur.ell[c0 + lane], sx0, sx1, sy0, sy1);
-                }
-            }
+            const bool hit = warp_hit(cur, c0, n, lane, sx0, sx1, sy0, sy1);
             unsigned mask = __ballot_sync(0xffffffffu, hit);
             while (mask) {
                 if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
