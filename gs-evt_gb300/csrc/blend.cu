@@ -310,6 +310,78 @@ __device__ __forceinline__ float warp_reduce_transposed(float (&v)[NV], int lane
     return v[0];
 }
 
+// One candidate of the tracker adjoint (grey, pair-loss gradient gC per pixel): the
+// forward's decisions as predicates, the state update, and the six terms (the five
+// power-gradient moments and the colour gradient), zero for a lane that does not blend it.
+__device__ __forceinline__ bool tracker_candidate(const Batch<false> &cur, int j, float pxf, float pyf, float Cimg,
+                                                  float gC, float &T, float &Pc, bool &done, float (&g)[6])
+{
+    const float4 A = cur.A[j], B = cur.B[j];
+    const float dx = A.x - pxf, dy = A.y - pyf;
+    const float power = gs_power(B.x, B.y, B.z, dx, dy);
+    const float araw = B.w * gs_expf(power);
+    const float alpha = fminf(0.99f, araw);
+    const float test_T = T * (1.0f - alpha);
+    // A.z holds the Gaussian's power threshold in tracker mode
+    const bool pass = !done && !(power > 0.0f) && !(power < A.z) && !(alpha < 1.0f / 255.0f);
+    const bool stop = pass && test_T < 0.0001f;
+    const bool contrib = pass && !stop;
+    done = done || stop;
+    const float wgt = contrib ? alpha * T : 0.0f;
+    // gradient-only term: the 2-ulp fast reciprocal suffices
+    const float inv1m = __fdividef(1.0f, 1.0f - alpha);
+    Pc = contrib ? __fmaf_rn(A.w, wgt, Pc) : Pc;
+    const float dal = gC * __fmaf_rn(-(Cimg - Pc), inv1m, T * A.w);
+    // below the 0.99 clamp alpha depends on the power
+    const float dpow = (contrib && araw <= 0.99f) ? dal * araw : 0.0f;
+    const float mx = dpow * dx, my = dpow * dy;
+    g[0] = mx;
+    g[1] = my;
+    g[2] = mx * dx;
+    g[3] = mx * dy;
+    g[4] = my * dy;
+    g[5] = gC * wgt;
+    T = contrib ? test_T : T;
+    return contrib;
+}
+
+// Warp sums of the six terms of two candidates: the first stage trades candidate b of
+// lanes 0-15 for candidate a of lanes 16-31, then each half-warp reduces its candidate's
+// six values (padded to 8) transposed.  Lane l ends with the sum of term (l >> 1) & 7 of
+// candidate (l >> 4) (a for lanes 0-15).
+__device__ __forceinline__ float warp_reduce_pair6(const float (&a)[6], const float (&b)[6], int lane)
+{
+    const bool hi = (lane & 16) != 0;
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float send = hi ? a[k] : b[k];
+        const float keep = hi ? b[k] : a[k];
+        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    v[6] = v[7] = 0.0f;
+    int m = 8;
+#pragma unroll
+    for (int o = 8; o >= 1; o >>= 1) {
+        if (m > 1) {
+            const bool up = (lane & o) != 0;
+            const int half = m >> 1;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k < half) {
+                    const float send = up ? v[k] : v[half + k];
+                    const float keep = up ? v[half + k] : v[k];
+                    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+                }
+            }
+            m = half;
+        } else {
+            v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+        }
+    }
+    return v[0];
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
 {
@@ -396,6 +468,29 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
             const bool hit = warp_hit(cur, c0, n, lane, sx0, sx1, sy0, sy1);
             unsigned mask = __ballot_sync(0xffffffffu, hit);
+            if constexpr (MODE == 0) {
+                // the tracker adjoint takes its candidates two at a time: one 12-value warp
+                // reduction and one shared-memory atomic instruction for the pair
+                while (mask) {
+                    if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
+                    const int ja = c0 + __ffs(mask) - 1;
+                    mask &= mask - 1;
+                    const bool has_b = mask != 0u;
+                    const int jb = has_b ? c0 + __ffs(mask) - 1 : ja;
+                    if (has_b) mask &= mask - 1;
+                    float ga[6], gb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+                    const bool ca = tracker_candidate(cur, ja, pxf, pyf, Cimg[0], gC[0], T, Pc[0], done, ga);
+                    bool cb = false;
+                    if (has_b) cb = tracker_candidate(cur, jb, pxf, pyf, Cimg[0], gC[0], T, Pc[0], done, gb);
+                    if (__any_sync(0xffffffffu, ca || cb)) {
+                        const float s = warp_reduce_pair6(ga, gb, lane);
+                        const int q = (lane >> 1) & 7;
+                        const bool second = (lane & 16) != 0;
+                        if ((lane & 1) == 0 && q < NC && s != 0.0f && (has_b || !second))
+                            atomicAdd(&acc[second ? jb : ja][q], s);
+                    }
+                }
+            } else {
             while (mask) {
                 if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
                 const int j = c0 + __ffs(mask) - 1;
@@ -462,6 +557,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                     const int q = (lane >> SH) & (NV - 1);
                     if ((lane & ((1 << SH) - 1)) == 0 && q < NC && s != 0.0f) atomicAdd(&acc[j][q], s);
                 }
+            }
             }
         }
         __syncthreads();
