@@ -163,6 +163,43 @@ __device__ __forceinline__ void warp_pixel(int tid, int tx, int ty, int &px, int
     sy1 = (float)(by + 3);
 }
 
+// One candidate of the forward blend for one lane.  Every lane evaluates it and the
+// decisions are predicates (selects instead of divergent branches; stopped lanes change
+// nothing).  A candidate is skipped when power > 0 or below the Gaussian's alpha
+// threshold (it fails the alpha test anyway) or alpha < 1/255; the pixel stops before a
+// candidate that would take T below 1e-4.
+template <bool EXTRAS, bool RGB>
+__device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const BlendParams &p, int j, int r, float pxf,
+                                              float pyf, float &T, float &C0, float &C1, float &C2, float &D,
+                                              float &Aacc, int &last, bool &done)
+{
+    const float4 A = cur.A[j], B = cur.B[j];
+    const float dx = A.x - pxf, dy = A.y - pyf;
+    const float power = gs_power(B.x, B.y, B.z, dx, dy);
+    const float alpha = fminf(0.99f, B.w * gs_expf(power));
+    const float test_T = T * (1.0f - alpha);
+    const bool pass = !done && !(power > 0.0f) && !(power < (EXTRAS ? cur.ell[j].w : A.z)) &&
+                      !(alpha < 1.0f / 255.0f);
+    const bool stop = pass && test_T < 0.0001f;
+    const bool use = pass && !stop;
+    done = done || stop;
+    if (RGB) {
+        const float4 Cc = cur.C[j];
+        C0 = use ? fmaf(Cc.x * alpha, T, C0) : C0;
+        C1 = use ? fmaf(Cc.y * alpha, T, C1) : C1;
+        C2 = use ? fmaf(Cc.z * alpha, T, C2) : C2;
+    } else {
+        C0 = use ? fmaf(A.w * alpha, T, C0) : C0;
+    }
+    if (EXTRAS) {
+        D = use ? fmaf(A.z * alpha, T, D) : D;
+        Aacc = use ? fmaf(alpha, T, Aacc) : Aacc;
+        if (use && p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
+        last = use ? r * GS_BLOCK + j + 1 : last;
+    }
+    T = use ? test_T : T;
+}
+
 // EXTRAS: the frame wants depth, alpha, contributor counts or n_touched (each still
 // checked at run time); without it only the image and the final transmittance are
 // accumulated (the batched tracker's case).
@@ -211,40 +248,16 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
             // candidates of this warp among the next 32 Gaussians, in depth order
             const bool hit = warp_hit(cur, c0, n, lane, sx0, sx1, sy0, sy1);
             unsigned mask = __ballot_sync(0xffffffffu, hit);
+            // candidates two at a time (one saturation vote and loop step per pair)
             while (mask) {
                 if (__all_sync(0xffffffffu, done)) { warp_done = true; break; }
-                const int j = c0 + __ffs(mask) - 1;
+                fwd_candidate<EXTRAS, RGB>(cur, p, c0 + __ffs(mask) - 1, r, pxf, pyf, T, C0, C1, C2, D, Aacc, last, done);
                 mask &= mask - 1;
-                // Every lane evaluates the candidate and the decisions become predicates
-                // (selects instead of divergent branches; stopped lanes change nothing).
-                // A candidate is skipped when power > 0 or below the Gaussian's alpha
-                // threshold (it fails the alpha test anyway) or alpha < 1/255; the pixel
-                // stops before a candidate that would take T below 1e-4.
-                const float4 A = cur.A[j], B = cur.B[j];
-                const float dx = A.x - pxf, dy = A.y - pyf;
-                const float power = gs_power(B.x, B.y, B.z, dx, dy);
-                const float alpha = fminf(0.99f, B.w * gs_expf(power));
-                const float test_T = T * (1.0f - alpha);
-                const bool pass = !done && !(power > 0.0f) && !(power < (EXTRAS ? cur.ell[j].w : A.z)) &&
-                                  !(alpha < 1.0f / 255.0f);
-                const bool stop = pass && test_T < 0.0001f;
-                const bool use = pass && !stop;
-                done = done || stop;
-                if (RGB) {
-                    const float4 Cc = cur.C[j];
-                    C0 = use ? fmaf(Cc.x * alpha, T, C0) : C0;
-                    C1 = use ? fmaf(Cc.y * alpha, T, C1) : C1;
-                    C2 = use ? fmaf(Cc.z * alpha, T, C2) : C2;
-                } else {
-                    C0 = use ? fmaf(A.w * alpha, T, C0) : C0;
+                if (mask) {
+                    fwd_candidate<EXTRAS, RGB>(cur, p, c0 + __ffs(mask) - 1, r, pxf, pyf, T, C0, C1, C2, D, Aacc, last,
+                                               done);
+                    mask &= mask - 1;
                 }
-                if (EXTRAS) {
-                    D = use ? fmaf(A.z * alpha, T, D) : D;
-                    Aacc = use ? fmaf(alpha, T, Aacc) : Aacc;
-                    if (use && p.n_touched && test_T > 0.5f) atomicAdd(p.n_touched + cur.id[j], 1);
-                    last = use ? r * GS_BLOCK + j + 1 : last;
-                }
-                T = use ? test_T : T;
             }
         }
         __syncthreads();  // the next iteration overwrites this buffer
