@@ -26,8 +26,9 @@
 
 // ----------------------------------------------------------------- exp ----------
 // Deterministic exp for x <= 0: Cody & Waite (1980) reduction x = k ln2 + r with a
-// two-part ln2, degree-7 Taylor polynomial of e^r (Horner, fused multiply-adds) and an
-// exact power-of-two scale.  Bit-identical to or_expf in the CPU oracle.  Returns 0 for
+// two-part ln2, e^r = 1 + r + r^2 q(r) with q a degree-4 near-minimax polynomial (Lawson
+// fit, oracle/fit_exp.py; Horner with fused multiply-adds) and an exact power-of-two
+// scale: below 0.88 ulp.  Bit-identical to or_expf in the CPU oracle.  Returns 0 for
 // x < -87 and for NaN.
 __host__ __device__ __forceinline__ float gs_expf(float x)
 {
@@ -35,12 +36,11 @@ __host__ __device__ __forceinline__ float gs_expf(float x)
     float k = rintf(x * 0x1.715476p+0f);
     float r = fmaf(k, -0x1.62e4p-1f, x);
     r = fmaf(k, -0x1.7f7d1cp-20f, r);
-    float p = 0x1.a01a02p-13f;
-    p = fmaf(p, r, 0x1.6c16c2p-10f);
-    p = fmaf(p, r, 0x1.111112p-7f);
-    p = fmaf(p, r, 0x1.555556p-5f);
-    p = fmaf(p, r, 0x1.555556p-3f);
-    p = fmaf(p, r, 0.5f);
+    float p = 0x1.6a2444p-10f;
+    p = fmaf(p, r, 0x1.1239d6p-7f);
+    p = fmaf(p, r, 0x1.5558f2p-5f);
+    p = fmaf(p, r, 0x1.555492p-3f);
+    p = fmaf(p, r, 0x1.fffffcp-2f);
     p = fmaf(p, r, 1.0f);
     p = fmaf(p, r, 1.0f);
     int ki = (int)k;

@@ -38,22 +38,22 @@
 /* ---------------------------------------------------------------- exp -------- */
 /* Deterministic exp for x <= 0 used by the blending stages on both CPU and GPU.
  * Method: Cody & Waite (1980) argument reduction x = k ln2 + r with ln2 split into a
- * short high part (exact products k*LN2_HI for |k| < 2^9) and a low correction,
- * followed by the degree-7 Taylor polynomial of e^r on |r| <= ln2/2 evaluated with
- * fused multiply-adds, and an exact power-of-two scale.  Max error < 2 ulp
- * (checked against numpy in tests/test_oracle.py).  Returns 0 for x < -87 and NaN. */
+ * short high part (exact products k*LN2_HI for |k| < 2^9) and a low correction, then
+ * e^r = 1 + r + r^2 q(r) on |r| <= ln2/2 with q a degree-4 near-minimax polynomial
+ * (Lawson's reweighted least squares, oracle/fit_exp.py) evaluated with fused
+ * multiply-adds, and an exact power-of-two scale.  Max error < 0.88 ulp (checked
+ * against numpy in tests/test_oracle.py).  Returns 0 for x < -87 and NaN. */
 static float or_expf(float x)
 {
     if (!(x >= -87.0f)) return 0.0f;
     float k = rintf(x * 0x1.715476p+0f);
     float r = fmaf(k, -0x1.62e4p-1f, x);
     r = fmaf(k, -0x1.7f7d1cp-20f, r);
-    float p = 0x1.a01a02p-13f;
-    p = fmaf(p, r, 0x1.6c16c2p-10f);
-    p = fmaf(p, r, 0x1.111112p-7f);
-    p = fmaf(p, r, 0x1.555556p-5f);
-    p = fmaf(p, r, 0x1.555556p-3f);
-    p = fmaf(p, r, 0.5f);
+    float p = 0x1.6a2444p-10f;
+    p = fmaf(p, r, 0x1.1239d6p-7f);
+    p = fmaf(p, r, 0x1.5558f2p-5f);
+    p = fmaf(p, r, 0x1.555492p-3f);
+    p = fmaf(p, r, 0x1.fffffcp-2f);
     p = fmaf(p, r, 1.0f);
     p = fmaf(p, r, 1.0f);
     int ki = (int)k;

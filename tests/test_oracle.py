@@ -24,7 +24,7 @@ def test_expf_error_bound():
     got = np.array([oracle.expf(x) for x in xs], np.float64)
     ref = np.exp(xs.astype(np.float64))
     ulp = np.abs(got - ref) / np.spacing(np.float32(ref).astype(np.float32)).astype(np.float64)
-    assert ulp.max() <= 2.0, ulp.max()
+    assert ulp.max() <= 1.0, ulp.max()
     assert oracle.expf(-88.0) == 0.0 and oracle.expf(float("nan")) == 0.0
 
 
