@@ -67,15 +67,13 @@ template <bool RGB> struct Batch {
 // only if alpha = min(0.99, o exp(power)) >= 1/255, i.e. -power <= tau = ln(255 o).  With
 // M the conic, -power = d^T M d / 2 in exact arithmetic; the FP32 evaluation (gs_power:
 // five products and two fused multiply-adds) deviates by less than 1e-6 tr(M) |d|^2, so
-// every pixel that can pass satisfies Q(d) = d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the slack also covers
-// gs_expf's 2 ulp and logf).  The box of that ellipse, widened by 0.1 % + 0.5 px,
+// every pixel that can pass satisfies Q(d) = d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the
+// slack also covers gs_expf's and logf's rounding).  The box of that ellipse, widened by 0.1 % + 0.5 px,
 // therefore never excludes a pixel whose per-pixel test would pass, so culling against it
 // leaves every blending decision - and the result bits - unchanged.
 // Also returns, through *ell, Q's coefficients {a, b, c} (Q = a dx^2 + 2 b dx dy + c dy^2;
-// all zero when Q is ill-conditioned, which disables the ellipse test) and a power
-// threshold thr: below -(ln(255 o) (1 + 1e-4) + 1e-3), o exp(power) < 0.999 / 255, so
-// alpha < 1/255 whatever exp's last bits - the exp and the alpha test can be skipped there
-// without changing any decision.
+// all zero when Q is ill-conditioned, which disables the ellipse test) and -tau with tau
+// = ln(255 o) (1 + 1e-4) + 1e-3 (1e30 when no pixel can pass), the ellipse test's bound.
 __device__ __forceinline__ float4 gauss_box(float4 A, float4 B, float4 *ell)
 {
     const float o = B.w;
@@ -165,9 +163,8 @@ __device__ __forceinline__ void warp_pixel(int tid, int tx, int ty, int &px, int
 
 // One candidate of the forward blend for one lane.  Every lane evaluates it and the
 // decisions are predicates (selects instead of divergent branches; stopped lanes change
-// nothing).  A candidate is skipped when power > 0 or below the Gaussian's alpha
-// threshold (it fails the alpha test anyway) or alpha < 1/255; the pixel stops before a
-// candidate that would take T below 1e-4.
+// nothing).  A candidate is skipped when power > 0 or alpha < 1/255; the pixel stops
+// before a candidate that would take T below 1e-4.
 template <bool EXTRAS, bool RGB>
 __device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const BlendParams &p, int j, int r, float pxf,
                                               float pyf, float &T, float &C0, float &C1, float &C2, float &D,
@@ -178,8 +175,7 @@ __device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const Blend
     const float power = gs_power(B.x, B.y, B.z, dx, dy);
     const float alpha = fminf(0.99f, B.w * gs_expf(power));
     const float test_T = T * (1.0f - alpha);
-    const bool pass = !done && !(power > 0.0f) && !(power < (EXTRAS ? cur.ell[j].w : A.z)) &&
-                      !(alpha < 1.0f / 255.0f);
+    const bool pass = !done && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
     const bool stop = pass && test_T < 0.0001f;
     const bool use = pass && !stop;
     done = done || stop;
@@ -240,7 +236,6 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
             float4 e;
             cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &e);
             cur.ell[threadIdx.x] = e;
-            if (!EXTRAS) cur.A[threadIdx.x].z = e.w;  // depth is not needed: keep the threshold in its slot
         }
         __syncthreads();
         bool warp_done = false;
@@ -335,8 +330,7 @@ __device__ __forceinline__ bool tracker_candidate(const Batch<false> &cur, int j
     const float araw = B.w * gs_expf(power);
     const float alpha = fminf(0.99f, araw);
     const float test_T = T * (1.0f - alpha);
-    // A.z holds the Gaussian's power threshold in tracker mode
-    const bool pass = !done && !(power > 0.0f) && !(power < A.z) && !(alpha < 1.0f / 255.0f);
+    const bool pass = !done && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
     const bool stop = pass && test_T < 0.0001f;
     const bool contrib = pass && !stop;
     done = done || stop;
@@ -474,7 +468,6 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
             float4 e;
             cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &e);
             cur.ell[threadIdx.x] = e;
-            if (MODE == 0) cur.A[threadIdx.x].z = e.w;  // the tracker adjoint needs no depth
         }
         __syncthreads();
         bool warp_done = false;
@@ -517,8 +510,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                 const float araw = B.w * G;
                 const float alpha = fminf(0.99f, araw);
                 const float test_T = T * (1.0f - alpha);
-                const bool pass = !done && !(power > 0.0f) && !(power < (MODE != 0 ? cur.ell[j].w : A.z)) &&
-                                  !(alpha < 1.0f / 255.0f);
+                const bool pass = !done && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
                 const bool stop = pass && test_T < 0.0001f;
                 const bool contrib = pass && !stop;
                 done = done || stop;
