@@ -252,7 +252,9 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
     cudaMemsetAsync(ws.sort_hist, 0, GS_MAX_PASSES * 256 * 4, s);
     cudaMemsetAsync(ws.sort_counter, 0, GS_MAX_PASSES * 4, s);
     GS_CUDA_CHECK();
-    int hblocks = (int)std::min<uint32_t>((max_keys + 1023) / 1024, 152u * 4u);
+    // ~4096 keys per block, at most two blocks per SM: each block flushes up to 256 bins per
+    // pass to the global histogram with atomics, so fewer, fuller blocks flush less
+    int hblocks = (int)std::min<uint32_t>((max_keys + 4095) / 4096, 152u * 2u);
     k_sort_hist<KT><<<hblocks, 256, 0, s>>>(keys[0], count, capacity, passes, ws.sort_hist, ws.status);
     GS_CUDA_CHECK();
     // resident blocks per SM of the pass kernel (registers / shared memory bound)
