@@ -80,14 +80,17 @@ def _ws_region(frame, name, dtype, count):
     return frame.workspace[off:off + nbytes].view(dtype)
 
 
-@pytest.mark.parametrize("sizes", [((320, 240, 300.0), (256, 192, 220.0)), ((640, 480, 600.0), (1280, 720, 900.0))])
+@pytest.mark.parametrize("sizes", [((320, 240, 300.0, 20000), (256, 192, 220.0, 15000)),
+                                   ((640, 480, 600.0, 20000), (1280, 720, 900.0, 15000)),
+                                   ((64, 48, 60.0, 60000), (96, 64, 80.0, 40000))])
 def test_super_tile_lists_match_tile_sort(sizes):
     """The batched step bins through 4x4-tile super-tiles; its per-tile lists, ranges and
-    images equal the full stable tile sort of gsevt_bin_and_sort on the same views."""
-    (w0, h0, f0), (w1, h1, f1) = sizes
-    s0, pk0, sig0, _, _ = _scenario(20000, w0, h0, f0, 5, 30000)
-    s1, pk1, sig1, _, _ = _scenario(15000, w1, h1, f1, 6, 30000)
-    maps = [{"packed": pk0, "n": 20000}, {"packed": pk1, "n": 15000}]
+    images equal the full stable tile sort of gsevt_bin_and_sort on the same views (the
+    third case: small dense views whose single super-tiles hold 20-34k Gaussians)."""
+    (w0, h0, f0, n0), (w1, h1, f1, n1) = sizes
+    s0, pk0, sig0, _, _ = _scenario(n0, w0, h0, f0, 5, 30000)
+    s1, pk1, sig1, _, _ = _scenario(n1, w1, h1, f1, 6, 30000)
+    maps = [{"packed": pk0, "n": n0}, {"packed": pk1, "n": n1}]
     def prob(sc, mi, E, seed):
         R, t = synthetic.perturb(sc.gt_R, sc.gt_t, np.random.default_rng(seed), 0.05, 3.0)
         c = sc.camera
