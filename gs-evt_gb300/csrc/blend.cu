@@ -20,14 +20,17 @@
 // The power's gradient enters the 2D mean and conic gradients linearly in the conic, so a
 // pixel contributes the five moments dpow (dx, dy, dx^2, dx dy, dy^2) and the conic is
 // applied once per Gaussian and tile.  Per-Gaussian contributions are reduced across the
-// warp in FP32 (shuffles), summed per tile in shared memory and added to the global
-// per-slot gradients once per tile.
+// warp in FP32 (shuffles; the tracker adjoint reduces two candidates' terms per butterfly),
+// summed per tile in shared memory and added to the global per-slot gradients once per
+// tile.
 //
 // Warp-level culling (both directions): each batch Gaussian gets a conservative pixel
 // box and quadratic form of its alpha support (gauss_box); a warp ballots which of them
 // reach its 8x4 pixel block (box overlap, then the exact ellipse-rectangle test of
-// ellipse_hits) and walks only those, in depth order.  Gaussians that fail both cannot
-// pass the per-pixel alpha test, so the decisions and results are unchanged.
+// ellipse_hits) and walks only those, in depth order, two at a time.  Gaussians that fail
+// both cannot pass the per-pixel alpha test, so the decisions and results are unchanged.
+// Every lane evaluates each candidate; the per-pixel decisions are predicates, not
+// divergent branches.
 #include "common.cuh"
 
 namespace {
@@ -59,7 +62,7 @@ template <bool RGB> struct Batch {
     float4 B[GS_BLOCK];
     float4 C[RGB ? GS_BLOCK : 1];
     float4 box[GS_BLOCK];  // {xmin, xmax, ymin, ymax}: outside it the Gaussian fails the alpha test
-    float4 ell[GS_BLOCK];  // {a, b, c, thr}: quadratic form of the support and power threshold
+    float4 ell[GS_BLOCK];  // {a, b, c, -tau}: quadratic form of the alpha support and its bound
     uint32_t id[GS_BLOCK];
 };
 
