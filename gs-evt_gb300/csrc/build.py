@@ -3,7 +3,8 @@
 Each .cu file is compiled to an object in parallel, then linked into
 gs-evt_gb300/gsevt/_build/libgsevt.so.  -fmad=false keeps every multiply and add
 separately rounded unless the source writes fmaf(), which is what makes the forward
-stages bit-identical to the CPU oracle.
+stages bit-identical to the CPU oracle.  The files in CONTRACT hold only gradient and pose
+arithmetic (parity is a tolerance there) and are compiled with contraction allowed.
 """
 import concurrent.futures as cf
 import os
@@ -15,8 +16,9 @@ PKG = os.path.dirname(HERE)
 REPO = os.path.dirname(PKG)
 OUT_DIR = os.path.join(PKG, "gsevt", "_build")
 LIB = os.path.join(OUT_DIR, "libgsevt.so")
-SOURCES = ["preprocess.cu", "binning.cu", "sort.cu", "blend.cu", "loss.cu", "track.cu", "events.cu",
-           "capi.cu"]
+SOURCES = ["preprocess.cu", "preprocess_cached.cu", "binning.cu", "sort.cu", "blend.cu", "loss.cu", "track.cu",
+           "events.cu", "capi.cu"]
+CONTRACT = {"preprocess_cached.cu", "track.cu"}
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
          "-Xcompiler", "-fPIC", "-I", os.path.join(REPO, "include"), "-I", HERE]
@@ -35,7 +37,8 @@ def build(force=False, verbose=False, extra_flags=()):
 
     def compile_one(src):
         obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
-        cmd = [NVCC, *FLAGS, *extra_flags, "-c", os.path.join(HERE, src), "-o", obj]
+        flags = [("-fmad=true" if f == "-fmad=false" and src in CONTRACT else f) for f in FLAGS]
+        cmd = [NVCC, *flags, *extra_flags, "-c", os.path.join(HERE, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
