@@ -32,8 +32,9 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
 
 namespace {
 
-// exclusive scan of n block sums (one block of 1024 threads); total into *total and an
-// overflow flag when the total exceeds `capacity` (0: no check)
+// exclusive scan of n block sums (one block of 1024 threads; shuffle scans within warps
+// and over the warp totals); total into *total and an overflow flag when the total exceeds
+// `capacity` (0: no check)
 __device__ void scan_blocks(const uint32_t *sums, uint32_t *offs, int n, uint32_t *total, uint32_t *status,
                             uint32_t capacity, unsigned long long *part);
 __global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t *sums, uint32_t *offs, int n, uint32_t *total,
@@ -59,26 +60,39 @@ __global__ void __launch_bounds__(1024) k_scan_blocks2(const uint32_t *sums, uin
 __device__ void scan_blocks(const uint32_t *sums, uint32_t *offs, int n, uint32_t *total, uint32_t *status,
                             uint32_t capacity, unsigned long long *part)
 {
-    int t = threadIdx.x;
-    int per = (n + 1023) / 1024;
-    int b = t * per, e = min(n, b + per);
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int per = (n + 1023) / 1024;
+    const int b = t * per, e = min(n, b + per);
     unsigned long long s = 0;
     for (int i = b; i < e; ++i) s += sums[i];
-    part[t] = s;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        unsigned long long v = t >= o ? part[t - o] : 0ull;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+    // warp-shuffle scan of the 1024 thread sums (64-bit), then of the 32 warp totals
+    unsigned long long inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
     }
-    unsigned long long run = t > 0 ? part[t - 1] : 0ull;
+    if (lane == 31) part[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const unsigned long long v = part[lane];
+        unsigned long long wi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        part[lane] = wi - v;
+        if (lane == 31) part[32] = wi;
+    }
+    __syncthreads();
+    unsigned long long run = part[w] + inc - s;
     for (int i = b; i < e; ++i) {
         offs[i] = (uint32_t)min(run, 0xffffffffull);
         run += sums[i];
     }
-    if (t == 1023) {
-        unsigned long long tot = part[1023];
+    if (t == 0) {
+        const unsigned long long tot = part[32];
         *total = (uint32_t)min(tot, 0xffffffffull);
         if (capacity && tot > capacity) atomicOr(&status[0], GSEVT_STATUS_KEY_OVERFLOW);
     }
