@@ -231,11 +231,25 @@ class BatchedSequenceTracker:
     def _host_states(self):
         return self.state.view(torch.uint8).cpu().numpy().copy()
 
-    def track(self, init_states, windows):
+    def _write_overlay(self, overlay_dir, pi, slot, fi):
+        import os
+        from . import io as gio
+        fr = self.trackers[0].frame
+        d = fr.pixels(2 * slot + 1)[0] - fr.pixels(2 * slot)[0]  # I_next - I_last (frame.py:86-94)
+        n = d / torch.linalg.vector_norm(d)
+        mi, W, H, fx, fy = self.cameras[pi]
+        e = self.ev[0][slot][0].view(H, W)
+        path = os.path.join(overlay_dir, "problem_%d" % pi)
+        os.makedirs(path, exist_ok=True)
+        gio.write_png(os.path.join(path, "frame_%d.png" % fi), gio.event_overlay(e, n))
+
+    def track(self, init_states, windows, overlay_dir=None):
         """init_states: per problem (R, t, lin_vel, ang_vel) (world -> camera, FP64);
         windows: per frame, a list with one EventArray per problem (or a tuple
         (x, y, polarity, ts, camera_or_None)).  Returns per problem a list of
-        (timestamp, R, t)."""
+        (timestamp, R, t).  overlay_dir: if given, each frame's tracking image (the signed
+        event frame over the last finest-level render difference, utils/tracker.py:267-270)
+        is written to overlay_dir/problem_<i>/frame_<f>.png."""
         from .events import event_frames
         from .pose import exp_se3, matrix, so3_log
         n = self.num
@@ -343,6 +357,8 @@ class BatchedSequenceTracker:
                 last_dtau[slot] = dtau
                 stamp = (ts[0] + (ts[-1] - ts[0]) / 2) / 1e6 if len(ts) else 0.0
                 traj[pi].append((stamp, np.asarray(s.R[:]).reshape(3, 3).copy(), np.asarray(s.t[:]).copy()))
+                if overlay_dir is not None:
+                    self._write_overlay(overlay_dir, pi, slot, fi)
         self.state.copy_(torch.frombuffer(bytearray(bytes(host)), dtype=torch.uint8))
         # Adam iterations each problem ran (a frozen problem does not count)
         self.problem_iterations = [0] * n

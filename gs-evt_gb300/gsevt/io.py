@@ -8,7 +8,15 @@
 - `load_events_txt`: "ts x y polarity" integer lines chunked into windows of
   max_events_per_frame events, leftover events dropped (utils/event_camera/event.py:11-39).
 - `write_tum`: "timestamp tx ty tz qx qy qz qw" lines (utils/tracker.py:258-265).
+- `event_overlay` / `write_png`: the per-frame tracking image of utils/tracker.py:267-270
+  (utils/visualizer.py:7-44): the signed event frame in red (positive) and blue
+  (negative) over the signed normalised render difference in grey, 60 / 40, written as a
+  PNG.  The video and GIF assembly of utils/tracker.py:281-285 needs an encoder (cv2,
+  PIL) and is not provided.
 """
+import struct
+import zlib
+
 import numpy as np
 
 from .events import EventArray
@@ -146,11 +154,94 @@ def rotation_to_quaternion_xyzw(R):
     return q / np.linalg.norm(q)
 
 
+def _quaternion_xyzw(R):
+    # the reference converts with scipy's Rotation.from_matrix(R).as_quat()
+    # (utils/tracker.py:261-262); without scipy, Shepperd's method
+    try:
+        from scipy.spatial.transform import Rotation
+    except ImportError:
+        return rotation_to_quaternion_xyzw(R)
+    return Rotation.from_matrix(np.asarray(R)).as_quat()
+
+
 def write_tum(path, trajectory):
     """trajectory: iterable of (timestamp, R (world->camera rotation), t) as the tracker
-    returns them; written as the reference does (translation and quaternion of R, t)."""
+    returns them; written as the reference does (utils/tracker.py:258-265): translation and
+    quaternion (x, y, z, w) of R, t, each number printed as its numpy scalar (so a float32
+    translation prints as float32)."""
     with open(path, "w") as f:
         for ts, R, t in trajectory:
-            q = rotation_to_quaternion_xyzw(R)
-            t = np.asarray(t, np.float64).reshape(3)
-            f.write("%s %s %s %s %s %s %s %s\n" % (ts, t[0], t[1], t[2], q[0], q[1], q[2], q[3]))
+            q = _quaternion_xyzw(R)
+            t = np.asarray(t).reshape(3)
+            f.write(f"{ts} {t[0]} {t[1]} {t[2]} {q[0]} {q[1]} {q[2]} {q[3]}\n")
+
+
+def _scaled(x):
+    # x * (255 / max |x|) in the array's precision (utils/visualizer.py:14-17, 31-34)
+    x = np.asarray(x)
+    m = max(x.max(), abs(x.min())) if x.size else 0
+    if not m > 0:
+        return np.zeros_like(x)
+    return x * (x.dtype.type(255) / m)
+
+
+def event_overlay(sign_delta_Ie, sign_delta_Ir):
+    """The tracking image of one frame as a BGR uint8 [H, W, 3] array, as the reference
+    builds it: get_delta_Ie_img (positive events in the red channel, negative in blue,
+    values scaled to 255 by the largest magnitude and truncated), get_delta_Ir_img (grey
+    (d + 255) / 2 of the scaled render difference, truncated) and overlay_two_imgs
+    (0.6 events + 0.4 render, rounded half to even and saturated, as cv2.addWeighted).
+    Inputs: [H, W] (or [1, H, W]) arrays or tensors."""
+    def host(a):
+        if hasattr(a, "detach"):
+            a = a.detach().cpu().numpy()
+        a = np.asarray(a)
+        return a.reshape(a.shape[-2], a.shape[-1])
+    e = _scaled(host(sign_delta_Ie))
+    ev = np.zeros(e.shape + (3,), np.uint8)
+    ev[..., 2] = np.where(e > 0, e, 0).astype(np.uint8)   # red: positive (BGR order)
+    ev[..., 0] = (-np.where(e < 0, e, 0)).astype(np.uint8)  # blue: negative
+    r = _scaled(host(sign_delta_Ir))
+    grey = ((r + r.dtype.type(255)) / r.dtype.type(2)).astype(np.uint8)
+    rd = np.repeat(grey[..., None], 3, axis=2)
+    mix = ev.astype(np.float32) * np.float32(0.6) + rd.astype(np.float32) * np.float32(0.4)
+    return np.clip(np.rint(mix), 0, 255).astype(np.uint8)
+
+
+def write_png(path, bgr):
+    """Writes a BGR uint8 [H, W, 3] image as an 8-bit RGB PNG (the file cv2.imwrite makes
+    of it), with the standard library's zlib."""
+    bgr = np.asarray(bgr, np.uint8)
+    h, w = bgr.shape[:2]
+    rgb = np.ascontiguousarray(bgr[..., ::-1])
+    raw = b"".join(b"\x00" + rgb[y].tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        return (struct.pack(">I", len(data)) + tag + data +
+                struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF))
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))
+
+
+def read_png_rgb(path):
+    """Reads back an 8-bit RGB PNG with no row filters (as write_png makes them)."""
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, w, h = 8, b"", 0, 0
+    while pos < len(data):
+        n, tag = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        if tag == b"IHDR":
+            w, h = struct.unpack(">II", body[:8])
+        elif tag == b"IDAT":
+            idat += body
+        pos += 12 + n
+    rows = zlib.decompress(idat)
+    stride = 1 + 3 * w
+    out = np.frombuffer(rows, np.uint8).reshape(h, stride)
+    assert (out[:, 0] == 0).all()
+    return out[:, 1:].reshape(h, w, 3).copy()

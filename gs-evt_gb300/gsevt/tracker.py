@@ -6,6 +6,7 @@ steps torch.optim.Adam, exactly the reference's per-iteration structure.  The ba
 path (gsevt.batched) does the same iteration in one graph-captured launch sequence.
 """
 import logging
+import os
 
 import numpy as np
 import torch
@@ -93,8 +94,10 @@ class Tracker:
     """Tracker(config, event_arrays, viewpoint, gaussians, pipeline, background, device)
     .tracking() — per frame: constant-velocity prediction, event pyramid, coarse
     (pose, unsigned loss) then fine (pose + velocity, signed loss) Adam stages per
-    pyramid level with slope-based convergence (tracker.py:105-287).  Poses are
-    returned as a list of (timestamp, R, t) instead of being written to disk."""
+    pyramid level with slope-based convergence (tracker.py:105-287).  Poses are returned
+    as a list of (timestamp, R, t); with config["Tracking"]["save_path"] they are also
+    written as the reference writes them (tracking_pose_tum.txt, and one overlay image per
+    frame in tracking_frames/frame_<i>.png, utils/tracker.py:106-108, 258-270)."""
 
     def __init__(self, config, event_arrays, viewpoint, gaussians, pipeline, background, device="cuda"):
         self.config, self.event_arrays = config, event_arrays
@@ -110,6 +113,7 @@ class Tracker:
         self.lrs = {k: opt[k] for k in ("cam_rot_delta", "cam_trans_delta", "cam_w_delta", "cam_v_delta")}
         self.pyramid_lvl = 3
         self.log = logging.getLogger("gsevt.tracker")
+        self.save_path = (config.get("Tracking") or {}).get("save_path") if hasattr(config, "get") else None
         self.trajectory = []
         self.iterations = 0
 
@@ -123,9 +127,12 @@ class Tracker:
         return torch.norm(r)
 
     def tracking(self):
+        from . import io as gio
         vp = self.viewpoint
         last_delta_tau = 0.0
         fraction_num = self.max_optim_iter / 2
+        if self.save_path:
+            os.makedirs(os.path.join(self.save_path, "tracking_frames"), exist_ok=True)
         for frame_idx, ea in enumerate(self.event_arrays):
             optimizer = make_optimizer(vp, self.lrs)
             delta_tau = ea.duration()
@@ -145,8 +152,8 @@ class Tracker:
                     if opt_vel:
                         k = it - start_vel
                         frac = k / fraction_num if 1 <= k <= fraction_num else 1
-                    val, _ = plain_iteration(vp, self.gaussians, self.background, optimizer, lvl, opt_vel,
-                                             ef.sign_pyramid[lvl], ef.unsign_pyramid[lvl], frac, self.lrs)
+                    val, rf = plain_iteration(vp, self.gaussians, self.background, optimizer, lvl, opt_vel,
+                                              ef.sign_pyramid[lvl], ef.unsign_pyramid[lvl], frac, self.lrs)
                     self.iterations += 1
                     losses.append(val)
                     if self.check_convergence(losses, self.converged_threshold):
@@ -163,4 +170,10 @@ class Tracker:
                 vp.cal_weighted_velocity(initial, (delta_tau + last_delta_tau) / 2, 0.5)
             last_delta_tau = delta_tau
             self.trajectory.append((ea.time(), vp.R.detach().cpu().numpy(), vp.T.detach().cpu().numpy()))
+            if self.save_path:
+                # the last render of the finest level against the frame's signed event frame
+                img = gio.event_overlay(ef.sign_pyramid[0], rf.sign_delta_Ir)
+                gio.write_png(os.path.join(self.save_path, "tracking_frames", "frame_%d.png" % frame_idx), img)
+        if self.save_path:
+            gio.write_tum(os.path.join(self.save_path, "tracking_pose_tum.txt"), self.trajectory)
         return self.trajectory

@@ -239,16 +239,18 @@ def test_batched_converges_like_plain():
     assert dt < 1e-3 and dr < 0.05, (dt, dr)
 
 
-def test_plain_tracker_loop_runs():
+def test_plain_tracker_loop_runs(tmp_path):
     """Tracker(...).tracking() over two event windows: coarse and fine stages, convergence
-    checks, constant-velocity prediction; poses stay finite and move."""
+    checks, constant-velocity prediction; poses stay finite and move.  With a save path it
+    writes the reference's outputs: the TUM trajectory and one overlay PNG per frame."""
     sc, pk, sig, uns, ea = _scenario(8000, 160, 120, 150.0, 5, 20000)
     cam = sc.camera
     cfg = {"Event": {"img_width": cam.width, "img_height": cam.height, "gaussian_kernel_size": 9,
                      "intrinsic": {"data": [cam.fx, 0, cam.width / 2, 0, cam.fy, cam.height / 2, 0, 0, 1]},
                      "distortion_factors": [0, 0, 0, 0, 0]},
            "Optimizer": {"cam_rot_delta": 0.004, "cam_trans_delta": 0.004, "cam_w_delta": 0.002,
-                         "cam_v_delta": 0.002, "converged_threshold": 1e-4, "max_optim_iter": 12}}
+                         "cam_v_delta": 0.002, "converged_threshold": 1e-4, "max_optim_iter": 12},
+           "Tracking": {"save_path": str(tmp_path)}}
     c = Camera(torch.tensor(sc.init_R, dtype=torch.float32), torch.tensor(sc.init_t, dtype=torch.float32),
                torch.tensor(sc.init_ang, dtype=torch.float32), torch.tensor(sc.init_lin, dtype=torch.float32),
                cam.fovx, cam.fovy, cam.width, cam.height, device="cuda")
@@ -259,6 +261,12 @@ def test_plain_tracker_loop_runs():
     for ts, R, t in traj:
         assert np.all(np.isfinite(R)) and np.all(np.isfinite(t))
         assert abs(np.linalg.det(R) - 1.0) < 1e-4
+    from gsevt import io as gio
+    lines = open(tmp_path / "tracking_pose_tum.txt").read().splitlines()
+    assert len(lines) == 2 and all(len(l.split()) == 8 for l in lines)
+    for i in range(2):
+        img = gio.read_png_rgb(str(tmp_path / "tracking_frames" / ("frame_%d.png" % i)))
+        assert img.shape == (cam.height, cam.width, 3) and img.max() > 0
 
 
 def test_event_pyramid_levels_in_tracker_frame():
@@ -294,7 +302,7 @@ def _sequence(sc, pk, n, frames, n_events, seed):
 
 
 @pytest.mark.parametrize("threshold", [0.0, 1e9])
-def test_batched_sequence_tracker_matches_plain_tracker(threshold):
+def test_batched_sequence_tracker_matches_plain_tracker(threshold, tmp_path):
     """Per-frame loop (constant-velocity prediction, 3 pyramid levels, coarse/fine stages,
     velocity learning-rate ramp, iteration limits, slope convergence) on the device for
     three problems over two maps, against the plain Tracker run per problem.  The two
@@ -320,7 +328,12 @@ def test_batched_sequence_tracker_matches_plain_tracker(threshold):
     bst = BatchedSequenceTracker([{"packed": pk0, "n": 20000}, {"packed": pk1, "n": 15000}], cams,
                                  max_optim_iter=max_iter, converged_threshold=threshold, poll_every=1,
                                  device=DEV)
-    traj = bst.track(inits, wins)
+    traj = bst.track(inits, wins, overlay_dir=str(tmp_path))
+    from gsevt import io as gio
+    for pi, (mi, W, H, fx, fy) in enumerate(cams):
+        for k in range(frames):
+            img = gio.read_png_rgb(str(tmp_path / ("problem_%d" % pi) / ("frame_%d.png" % k)))
+            assert img.shape == (H, W, 3) and img.max() > 0
     for pi, (sc, win) in enumerate(((s0, w0), (s1, w1), (s0, w0))):
         cam = sc.camera
         R0, t0, lv, av = inits[pi]

@@ -80,3 +80,44 @@ def test_tum_writer(tmp_path):
     for Rm in (gpose.exp_so3([math.pi - 1e-3, 0.1, 0.0]), gpose.exp_so3([0.0, math.pi * 0.999, 0.0])):
         q = gio.rotation_to_quaternion_xyzw(Rm)
         assert abs(np.linalg.norm(q) - 1) < 1e-12
+
+
+def test_tum_writer_formats_numbers_as_the_reference(tmp_path):
+    """utils/tracker.py:264-265 formats the float32 translation and the quaternion with an
+    f-string of numpy scalars; the writer does the same, so a float32 translation keeps
+    exactly the float32 value."""
+    R = gpose.exp_so3([0.1, 0.2, -0.3]).astype(np.float32)
+    t = np.array([0.1, -0.2, 0.3], np.float32)
+    p = str(tmp_path / "traj32.txt")
+    gio.write_tum(p, [(1.25, R, t)])
+    fields = open(p).read().split()
+    assert fields[:4] == ["1.25", f"{t[0]}", f"{t[1]}", f"{t[2]}"]
+    assert [np.float32(float(v)) for v in fields[1:4]] == list(t)
+
+
+def test_event_overlay_known_answer():
+    """utils/visualizer.py: events scaled by 255 / max |E|, positive -> red, negative ->
+    blue (BGR image), truncated; render difference scaled the same way, grey (d + 255) / 2
+    truncated; 0.6 events + 0.4 render rounded half to even (cv2.addWeighted)."""
+    E = np.array([[1.0, -0.5, 0.0]], np.float32)
+    D = np.array([[0.5, -1.0, 0.0]], np.float32)
+    img = gio.event_overlay(E, D)
+    assert img.dtype == np.uint8 and img.shape == (1, 3, 3)
+    # events: (B, G, R) = (0, 0, 255), (127, 0, 0), (0, 0, 0); render grey 191, 0, 127
+    np.testing.assert_array_equal(img[0, 0], [76, 76, 229])   # 0.4*191 = 76.4; 0.6*255 + 76.4
+    np.testing.assert_array_equal(img[0, 1], [76, 0, 0])      # 0.6*127 = 76.2
+    np.testing.assert_array_equal(img[0, 2], [51, 51, 51])    # 0.4*127 = 50.8
+    # no events at all: an event image of zeros (the reference would divide by zero)
+    z = gio.event_overlay(np.zeros((2, 2), np.float32), D[:, :2].repeat(2, 0))
+    assert z.shape == (2, 2, 3)
+
+
+def test_png_round_trip(tmp_path):
+    rng = np.random.default_rng(3)
+    bgr = rng.integers(0, 256, size=(17, 23, 3), dtype=np.uint8)
+    p = str(tmp_path / "x.png")
+    gio.write_png(p, bgr)
+    raw = open(p, "rb").read()
+    assert raw[:8] == b"\x89PNG\r\n\x1a\n" and raw[12:16] == b"IHDR"
+    rgb = gio.read_png_rgb(p)
+    np.testing.assert_array_equal(rgb, bgr[..., ::-1])
