@@ -126,6 +126,8 @@ __global__ void k_ev_blur_v(const float *tmp, int W, int H, Kern k, float *blur,
     }
 }
 
+// Grid-wide: every block forms the same scale from the partial sums (same order, same
+// bits) and writes a grid-stride share of every pyramid level.
 __global__ void k_ev_normalize(const float *blur, const double *part, int nparts, int W, int H, int levels,
                                float *out_s, float *out_u)
 {
@@ -153,6 +155,13 @@ __global__ void k_ev_normalize(const float *blur, const double *part, int nparts
         }
         off += P;
     }
+}
+
+// blocks of the normalisation: one thread per level-0 pixel, at most 8 blocks per SM
+inline int ev_norm_blocks(int W, int H)
+{
+    const size_t P = (size_t)W * H;
+    return (int)std::min<size_t>((P + 255) / 256, 152 * 8);
 }
 
 }  // namespace
@@ -202,8 +211,8 @@ extern "C" int gsevt_events_accumulate(int64_t n, const uint16_t *x, const uint1
     }
     k_ev_blur_h<<<gh, 128, 0, s>>>(sc.img, width, height, k, sc.tmp);
     k_ev_blur_v<<<EV_PART_BLOCKS, 256, 0, s>>>(sc.tmp, width, height, k, sc.blur, sc.part);
-    k_ev_normalize<<<1, 1024, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height, levels, out_signed,
-                                      out_unsigned);
+    k_ev_normalize<<<ev_norm_blocks(width, height), 256, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height,
+                                                                 levels, out_signed, out_unsigned);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }
@@ -283,8 +292,8 @@ extern "C" int gsevt_events_accumulate_noalloc(int64_t n, const uint16_t *x, con
         k_ev_to_float<<<(int)std::min<size_t>((P + 255) / 256, 152 * 8), 256, 0, s>>>(sc.count, P, sc.img);
     k_ev_blur_h<<<gh, 128, 0, s>>>(sc.img, width, height, k, sc.tmp);
     k_ev_blur_v<<<EV_PART_BLOCKS, 256, 0, s>>>(sc.tmp, width, height, k, sc.blur, sc.part);
-    k_ev_normalize<<<1, 1024, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height, levels, out_signed,
-                                      out_unsigned);
+    k_ev_normalize<<<ev_norm_blocks(width, height), 256, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height,
+                                                                 levels, out_signed, out_unsigned);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }
