@@ -21,7 +21,7 @@ import helpers
 pytestmark = pytest.mark.gpu
 
 DEV = torch.device("cuda")
-IMG_ATOL, IMG_RTOL = 1e-5, 1e-4   # images (FP32), spec tolerance
+IMG_ATOL, IMG_RTOL = 1e-5, 1e-4   # images (FP32): the parity tolerance for floating-point images
 GRAD_RTOL = 1e-4                   # pose / velocity gradients (norm-relative)
 
 
