@@ -592,13 +592,16 @@ def main():
         except Exception:
             traffic = None
     # kernels per iteration of the batched step: preprocess, visible scan, compaction,
-    # depth sort (histogram, 4 passes), sorted sums, paired scan, coarse duplication,
-    # super-tile sort (histogram, passes, + a super-tile range kernel when there are two),
-    # tile filter, blend fwd, loss, blend bwd, preprocess bwd, finalize
+    # depth sort (one cooperative launch when the visible-slot capacity fits 8192 keys
+    # per SM, else a histogram and 4 onesweep passes), sorted sums, paired scan, coarse
+    # duplication, super-tile sort (histogram, passes, + a super-tile range kernel when
+    # there are two), tile filter, blend fwd, loss, blend bwd, preprocess bwd, finalize
     L = bt.frame.L
     nsup = L.super_tiles if L.super_tiles > 0 else L.total_tiles // 4 + L.num_views + 1
     super_passes = (max(1, int(nsup - 1).bit_length()) + 7) // 8
-    launches_per_iter = 18 + super_passes + (1 if super_passes > 1 else 0)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    depth_sort_launches = 1 if L.num_vg <= min(sms, 160) * 8192 else 5
+    launches_per_iter = 13 + depth_sort_launches + super_passes + (1 if super_passes > 1 else 0)
     it_bytes = iteration_bytes(prob, dev)
     it_gbs = it_bytes["bytes_per_iter"] * (1000.0 / ms) / 1e9
     line = {

@@ -56,6 +56,7 @@ extern "C" int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream)
     int st = check_frame(f, &ws);
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    gs_sort_prepare();
     cudaMemsetAsync(ws.status, 0, 64, s);
     cudaMemsetAsync(ws.sort_lookback, 0, (size_t)gs_lookback_tiles(f->L) * 256 * 8, s);
     if (f->L.num_pairs > 0) cudaMemsetAsync(ws.loss_done, 0, (size_t)f->L.num_pairs * 4, s);

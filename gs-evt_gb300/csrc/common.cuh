@@ -23,6 +23,13 @@
 #endif
 #define GS_MAX_PASSES 8
 #define GS_SPIN_LIMIT (1u << 22)
+// cooperative sort (all passes of a sort in one launch, one block per SM): threads per
+// block, keys per thread at most, keys per block at most, and the padded column count
+// of its digit-major count table (an upper bound on the grid)
+#define GS_COOP_THREADS 1024
+#define GS_COOP_KPT 8
+#define GS_COOP_TILE (GS_COOP_THREADS * GS_COOP_KPT)
+#define GS_COOP_GP 160
 
 // ----------------------------------------------------------------- exp ----------
 // Deterministic exp for x <= 0: Cody & Waite (1980) reduction x = k ln2 + r with a
@@ -92,7 +99,7 @@ struct Workspace {
     uint32_t *toffs;      // [sorted blocks]
     uint32_t *keys[2];    // [key_capacity] global tile id of each (tile, Gaussian) pair
     uint32_t *vals[2];    // [key_capacity] its (view, Gaussian) slot
-    uint32_t *sort_hist;      // [GS_MAX_PASSES][256]
+    uint32_t *sort_hist;      // [GS_MAX_PASSES][256]; the cooperative sort's [256][GS_COOP_GP] + [256]
     uint32_t *sort_counter;   // [GS_MAX_PASSES]
     unsigned long long *sort_lookback;  // [sort tiles][256]  {epoch:32 | flag:2 | count:30}
     uint2 *ranges;        // [total_tiles]
@@ -184,7 +191,7 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     w.keys[1] = (uint32_t *)take(cap * 4);
     w.vals[0] = (uint32_t *)take(cap * 4);
     w.vals[1] = (uint32_t *)take(cap * 4);
-    w.sort_hist = (uint32_t *)take(GS_MAX_PASSES * 256 * 4);
+    w.sort_hist = (uint32_t *)take((size_t)std::max(GS_MAX_PASSES, GS_COOP_GP + 1) * 256 * 4);
     w.sort_counter = (uint32_t *)take(GS_MAX_PASSES * 4);
     w.sort_lookback = (unsigned long long *)take((size_t)gs_lookback_tiles(L) * 256 * 8);
     w.ranges = (uint2 *)take((size_t)L.total_tiles * 8);
@@ -279,3 +286,6 @@ __device__ __forceinline__ double warp_sum_d(double v)
         cudaError_t _e = cudaGetLastError();                    \
         if (_e != cudaSuccess) return GSEVT_ERR_CUDA;           \
     } while (0)
+
+// Prepares the cooperative sort on the current device (sort.cu); outside stream capture.
+void gs_sort_prepare();

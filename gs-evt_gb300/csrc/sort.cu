@@ -228,7 +228,284 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
     }
 }
 
+// ------------------------------------------------------------- cooperative ---------
+// Sorts of at most G x GS_COOP_TILE keys with two or more passes run every pass in one
+// cooperative launch of G = (SMs x resident blocks) 1024-thread blocks.  Block b owns the
+// contiguous run [b TS, (b + 1) TS) of the keys, TS = ceil(K / G), the same run in every
+// pass.  A pass:
+//   1. the block ranks its run stably (warp w takes the w-th 32nd of the run in rounds of
+//      32 keys; the lanes holding the same digit are found with nine ballots, so ranks
+//      follow the input order) and writes its 256 digit counts into column b of a
+//      digit-major table [256][GS_COOP_GP];
+//   2. grid barrier; meanwhile the block orders its keys by digit in shared memory (the
+//      values were staged there in input order);
+//   3. block b scans rows b, b + G, ... of the table in place (exclusive prefix over the
+//      blocks) and writes each row's total;
+//   4. grid barrier; thread d reads row d's prefix at column b and the row totals, whose
+//      exclusive scan over the digits places the block's digit runs; the runs are written
+//      out, and a third barrier ends the pass before the next one reads them.
+// There is no histogram kernel, no per-pass launch and no look-back chain, and no block
+// reads more of the table than its own column and the rows it scans.  A pass whose digit
+// is constant is the identity permutation here as well.  Barriers are an arrival counter
+// (release add, acquire loads); every wait is bounded by GS_SPIN_LIMIT polls, after which
+// the block records GSEVT_STATUS_SORT_TIMEOUT and continues.  Data written by other blocks
+// in an earlier phase is read with ld.global.cg (L2), never through a stale L1 line.
+struct CoopParams {
+    uint32_t *keys[2];
+    uint32_t *vals[2];
+    uint32_t *cnt;          // [256][GS_COOP_GP] per-block digit counts, then [256] row totals
+    uint32_t *barrier;      // arrival counter, zero at launch
+    uint32_t *status;
+    const uint32_t *count;  // number of keys (device word)
+    uint32_t capacity;
+    int passes;
+};
+
+__device__ __forceinline__ void coop_arrive(uint32_t *ctr)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
+}
+
+__device__ __forceinline__ void coop_wait(const uint32_t *ctr, uint32_t target, uint32_t *status)
+{
+    if (threadIdx.x == 0) {
+        uint32_t spins = 0, v;
+        for (;;) {
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+            if (v >= target) break;
+            if (++spins > GS_SPIN_LIMIT) {
+                atomicOr(status, GSEVT_STATUS_SORT_TIMEOUT);
+                break;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// exclusive scan of one value per thread over threads 0-255 (the digits); every thread
+// of the block must call it
+__device__ __forceinline__ uint32_t coop_digit_scan(uint32_t v, uint32_t *wsc)
+{
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    uint32_t inc = v;
+    if (tid < 256) {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wsc[w] = inc;
+    }
+    __syncthreads();
+    uint32_t base = 0;
+    if (tid < 256)
+        for (int i = 0; i < w; ++i) base += wsc[i];
+    __syncthreads();  // wsc is reused by the next scan
+    return base + inc - v;
+}
+
+#define COOP_WARPS (GS_COOP_THREADS / 32)
+__global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
+{
+    extern __shared__ uint32_t coop_smem[];
+    // block-sorted keys and values, and the values staged in input order
+    uint32_t *skeys = coop_smem, *svals = coop_smem + GS_COOP_TILE, *sin = coop_smem + 2 * GS_COOP_TILE;
+    __shared__ uint32_t whist[COOP_WARPS][256];
+    __shared__ uint32_t qall[4][256];
+    __shared__ uint32_t gbase[256], dstart[256];
+    __shared__ uint32_t wsc[8];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int d = tid & 255, q = tid >> 8;  // digit and quarter (four threads per digit)
+    const uint32_t G = gridDim.x, b = blockIdx.x;
+    const uint32_t K = min(*p.count, p.capacity);
+    if (K == 0) return;  // uniform over the grid
+    if (K > G * (uint32_t)GS_COOP_TILE || G > GS_COOP_GP || G * COOP_WARPS < 256) {
+        // the launcher sizes the grid for the capacity, so this is unreachable
+        if (b == 0 && tid == 0) atomicOr(p.status, GSEVT_STATUS_KEY_OVERFLOW);
+        return;
+    }
+    uint32_t *row_tot = p.cnt + 256 * GS_COOP_GP;
+    const uint32_t TS = (K + G - 1) / G;
+    const uint32_t t0 = min(K, b * TS);
+    const uint32_t nb = min(K, t0 + TS) - t0;                  // keys of this block (<= GS_COOP_TILE)
+    const uint32_t span = (nb + COOP_WARPS - 1) / COOP_WARPS;  // keys of each warp (<= 32 GS_COOP_KPT)
+    const int rounds = (int)((span + 31) / 32);
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t nbar = 0;
+    for (int pass = 0; pass < p.passes; ++pass) {
+        const bool odd = (pass & 1) != 0;  // selects, not a dynamic index into the parameters
+        const uint32_t *kin = odd ? p.keys[1] : p.keys[0], *vin = odd ? p.vals[1] : p.vals[0];
+        uint32_t *kout = odd ? p.keys[0] : p.keys[1], *vout = odd ? p.vals[0] : p.vals[1];
+        const int shift = 8 * pass;
+        for (int i = tid; i < COOP_WARPS * 256; i += GS_COOP_THREADS) (&whist[0][0])[i] = 0;
+        // keys into registers, values staged in shared memory in input order
+        uint32_t key[GS_COOP_KPT], rank[GS_COOP_KPT];
+        uint32_t ok = 0;
+#pragma unroll
+        for (int k = 0; k < GS_COOP_KPT; ++k) {
+            const uint32_t o = (uint32_t)(k * 32 + lane), li = (uint32_t)w * span + o;
+            const bool v = o < span && li < nb;
+            key[k] = v ? __ldcg(kin + t0 + li) : 0u;
+            if (v) sin[li] = __ldcg(vin + t0 + li);
+            rank[k] = 0u;
+            ok |= (uint32_t)v << k;
+        }
+        __syncthreads();
+        // stable ranks within each warp's keys, per-warp digit counts
+#pragma unroll
+        for (int k = 0; k < GS_COOP_KPT; ++k) {
+            if (k < rounds) {  // uniform over the block
+                const bool valid = ((ok >> k) & 1u) != 0;
+                const uint32_t dg = (key[k] >> shift) & 255u;
+                // lanes with the same validity and the same eight digit bits
+                uint32_t peers = __ballot_sync(0xffffffffu, valid);
+                if (!valid) peers = ~peers;
+#pragma unroll
+                for (int bit = 0; bit < 8; ++bit) {
+                    const uint32_t m = __ballot_sync(0xffffffffu, (dg >> bit) & 1u);
+                    peers &= ((dg >> bit) & 1u) ? m : ~m;
+                }
+                const int leader = __ffs(peers) - 1;
+                uint32_t before = 0;
+                if (valid) before = whist[w][dg];
+                __syncwarp();
+                if (valid && lane == leader) whist[w][dg] = before + __popc(peers);
+                __syncwarp();
+                rank[k] = before + __popc(peers & lt);
+            }
+        }
+        __syncthreads();
+        // per digit: exclusive offsets over the warps (each quarter of the threads takes
+        // eight warps) and the block's count
+        {
+            uint32_t s = 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) s += whist[8 * q + i][d];
+            qall[q][d] = s;
+        }
+        __syncthreads();
+        uint32_t pre = 0, tot = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint32_t v = qall[i][d];
+            pre += i < q ? v : 0u;
+            tot += v;
+        }
+        {
+            uint32_t run = pre;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const uint32_t v = whist[8 * q + i][d];
+                whist[8 * q + i][d] = run;
+                run += v;
+            }
+        }
+        if (q == 0) p.cnt[(size_t)d * GS_COOP_GP + b] = tot;
+        coop_arrive(p.barrier);
+        ++nbar;
+        // while the other blocks arrive: this block's keys in digit order in shared memory
+        {
+            const uint32_t ds = coop_digit_scan(tot, wsc);
+            if (tid < 256) dstart[d] = ds;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < GS_COOP_KPT; ++k) {
+            if ((ok >> k) & 1u) {
+                const uint32_t dg = (key[k] >> shift) & 255u;
+                const uint32_t pos = dstart[dg] + whist[w][dg] + rank[k];
+                skeys[pos] = key[k];
+                svals[pos] = sin[(uint32_t)w * span + (uint32_t)(k * 32 + lane)];
+            }
+        }
+        coop_wait(p.barrier, nbar * G, p.status);
+        // rows b, b + G, ... of the table: exclusive prefix over the blocks, in place, and
+        // the row total (warp i takes row b + i G; lane l holds columns l, l + 32, ...)
+        {
+            const uint32_t r = b + (uint32_t)w * G;
+            if (r < 256) {
+                uint32_t *row = p.cnt + (size_t)r * GS_COOP_GP;
+                uint32_t v[GS_COOP_GP / 32];
+#pragma unroll
+                for (int c = 0; c < GS_COOP_GP / 32; ++c) {
+                    const uint32_t col = (uint32_t)(c * 32 + lane);
+                    v[c] = col < G ? __ldcg(row + col) : 0u;
+                }
+                uint32_t run = 0;
+#pragma unroll
+                for (int c = 0; c < GS_COOP_GP / 32; ++c) {
+                    const uint32_t col = (uint32_t)(c * 32 + lane);
+                    uint32_t inc = v[c];
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                        if (lane >= o) inc += y;
+                    }
+                    if (col < G) row[col] = run + inc - v[c];
+                    run += __shfl_sync(0xffffffffu, inc, 31);
+                }
+                if (lane == 0) row_tot[r] = run;
+            }
+        }
+        coop_arrive(p.barrier);
+        ++nbar;
+        coop_wait(p.barrier, nbar * G, p.status);
+        uint32_t A = 0, E = 0;
+        if (tid < 256) {
+            E = __ldcg(p.cnt + (size_t)d * GS_COOP_GP + b);
+            A = __ldcg(row_tot + d);
+        }
+        {
+            const uint32_t ga = coop_digit_scan(A, wsc);
+            if (tid < 256) gbase[d] = ga + E;
+        }
+        __syncthreads();
+        for (uint32_t i = tid; i < nb; i += GS_COOP_THREADS) {
+            const uint32_t kk = skeys[i];
+            const uint32_t dg = (kk >> shift) & 255u;
+            kout[gbase[dg] + (i - dstart[dg])] = kk;
+            vout[gbase[dg] + (i - dstart[dg])] = svals[i];
+        }
+        if (pass + 1 < p.passes) {
+            coop_arrive(p.barrier);
+            ++nbar;
+            coop_wait(p.barrier, nbar * G, p.status);
+        }
+    }
+}
+#undef COOP_WARPS
+
+// grid of the cooperative sort on each device: 0 not prepared, -1 unavailable
+int g_coop_grid[64];
+
+int coop_grid_query(int dev)
+{
+    int coop = 0, sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return -1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+    const int smem = 3 * GS_COOP_TILE * 4;
+    if (cudaFuncSetAttribute(k_sort_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return -1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sort_coop, GS_COOP_THREADS, smem) != cudaSuccess)
+        return -1;
+    // at most GS_COOP_GP table columns; at least 8 blocks, so 256 / G rows fit 32 warps
+    const int g = std::min(sms * per_sm, GS_COOP_GP);
+    return g >= 8 ? g : -1;
+}
+
 }  // namespace
+
+// Sets up the cooperative sort on the current device (function attributes and its grid);
+// called outside stream capture, e.g. when a workspace is initialised.  A sort launched
+// on a device that was never prepared (or that lacks cooperative launches) runs the
+// onesweep passes.
+void gs_sort_prepare()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); return; }
+    if (g_coop_grid[dev] == 0) g_coop_grid[dev] = coop_grid_query(dev);
+    cudaGetLastError();
+}
 
 // Sorts keys[0]/vals[0] (count in *count, a device word) on the low `bits` bits; the
 // result is in buffer index (passes & 1), returned through *out_buf.  max_keys bounds
@@ -249,6 +526,37 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
     *out_buf = passes & 1;
     if (max_keys > capacity) max_keys = capacity;
     if (max_keys == 0) return GSEVT_OK;
+    if (sizeof(KT) == 4 && passes >= 2 && !ranges) {
+        int dev = 0;
+        const int g = (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) ? g_coop_grid[dev] : -1;
+        if (g > 0 && (uint64_t)capacity <= (uint64_t)g * GS_COOP_TILE) {
+            cudaMemsetAsync(ws.sort_counter, 0, 4, s);
+            CoopParams cp;
+            cp.keys[0] = (uint32_t *)keys[0];
+            cp.keys[1] = (uint32_t *)keys[1];
+            cp.vals[0] = vals[0];
+            cp.vals[1] = vals[1];
+            cp.cnt = ws.sort_hist;
+            cp.barrier = ws.sort_counter;
+            cp.status = ws.status;
+            cp.count = count;
+            cp.capacity = capacity;
+            cp.passes = passes;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)g);
+            cfg.blockDim = dim3(GS_COOP_THREADS);
+            cfg.dynamicSmemBytes = 3 * GS_COOP_TILE * 4;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            if (cudaLaunchKernelEx(&cfg, k_sort_coop, cp) != cudaSuccess) return GSEVT_ERR_CUDA;
+            GS_CUDA_CHECK();
+            return GSEVT_OK;
+        }
+    }
     cudaMemsetAsync(ws.sort_hist, 0, GS_MAX_PASSES * 256 * 4, s);
     cudaMemsetAsync(ws.sort_counter, 0, GS_MAX_PASSES * 4, s);
     GS_CUDA_CHECK();

@@ -160,7 +160,8 @@ typedef struct gsevt_frame {
 /* ---- sizing ---- */
 size_t gsevt_workspace_bytes(const gsevt_layout *L);
 /* Zero the parts of a fresh workspace that must start at zero (status words, sort
- * look-back table, loss tickets, tile ranges).  Call once after allocating it. */
+ * look-back table, loss tickets, tile ranges) and set up the single-launch cooperative
+ * sort on the current device.  Call once after allocating it, outside stream capture. */
 int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream);
 /* sizeof of the ABI structs, for binding checks: view, map, map_grads, pair, layout,
  * frame, pose_state (7 entries).  Touches no GPU state. */
