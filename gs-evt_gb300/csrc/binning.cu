@@ -532,9 +532,12 @@ BinParams make_params(const gsevt_frame *f, const Workspace &ws)
 }  // namespace
 
 // After preprocess: visible-slot compaction, depth sort, key offsets in depth order.
-// Leaves the key count in status[1] (and flags overflow) and N_vis in status[5].
-int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s, bool coarse)
+// Leaves the key count in status[1] (and flags overflow) and N_vis in status[5].  With
+// coarse (the batched tracker), *binned (if given) says whether the depth sort's launch
+// also built the super-tile lists, so that gs_launch_bin_coarse only filters them.
+int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s, bool coarse, bool *binned)
 {
+    if (binned) *binned = false;
     const gsevt_layout &L = f->L;
     const uint32_t nb = gs_sorted_blocks(L);
     if (L.num_scan_blocks <= 0 || L.num_vg <= 0) {
@@ -548,13 +551,25 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
     k_scan_blocks<<<1, 1024, 0, s>>>(ws.vis_sums, ws.vis_offs, L.num_scan_blocks, ws.status + 5, ws.status, 0);
     k_compact<<<L.num_scan_blocks, GS_BLOCK, 0, s>>>(p);
     GS_CUDA_CHECK();
-    int buf = 0;
-    uint32_t *dk[2] = {ws.dkeys[0], ws.dkeys[1]};
-    uint32_t *dv[2] = {ws.dvals[0], ws.dvals[1]};
-    int st = gs_launch_sort_t<uint32_t>(dk, dv, ws.status + 5, (uint32_t)L.num_vg, 32, (uint32_t)L.num_vg,
-                                       GS_SORT_KPT_DEPTH, ws, &buf, s, nullptr, 0);
+    GsCoarseBin cb = {};
+    if (coarse && binned && gs_super_bits(L) <= 8 && L.total_tiles > 0) {
+        cb.views = f->views;
+        cb.num_views = L.num_views;
+        cb.bin = ws.bin;
+        cb.soffs = ws.soffs;
+        cb.sranges = ws.sranges;
+        cb.cvals = ws.vals[1];
+        cb.capacity = (uint32_t)L.key_capacity;
+        cb.super_bound = gs_super_bound(L);
+        cb.enabled = 1;
+    }
+    bool fused = false;
+    int st = gs_launch_depth_sort(ws, (uint32_t)L.num_vg, cb.enabled ? &cb : nullptr, &fused, s);
     if (st) return st;
-    if (buf != 0) return GSEVT_ERR_ARG;  // 4 passes: the result is back in buffer 0
+    if (fused) {
+        *binned = true;
+        return GSEVT_OK;
+    }
     if (coarse) {
         k_sorted_sums<true><<<nb, GS_BLOCK, 0, s>>>(p, ws.dvals[0]);
         k_scan_blocks2<<<1, 1024, 0, s>>>(ws.tsums, ws.toffs, ws.status + 1, ws.csums, ws.coffs, ws.status + 6,
@@ -597,7 +612,7 @@ int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, 
 // gs_launch_bin (depth order within a tile, ties in slot order); only the values are
 // produced (the blend reads no keys).  The fine list is returned through *fine_vals.
 int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, uint32_t **fine_vals,
-                         cudaStream_t s)
+                         cudaStream_t s, bool binned)
 {
     const gsevt_layout &L = f->L;
     *fine_vals = ws.vals[0];
@@ -608,6 +623,14 @@ int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max
     if (L.num_vg <= 0 || max_keys == 0 || L.total_tiles <= 0) {
         cudaMemsetAsync(ws.ranges, 0, (size_t)L.total_tiles * sizeof(uint2), s);
         GS_CUDA_CHECK();
+        return GSEVT_OK;
+    }
+    if (binned) {
+        // the depth sort's launch built the super-tile lists in vals[1] and their ranges
+        k_filter_tiles<<<nsup, FILTER_WARPS * 32, 0, s>>>(f->views, L.num_views, ws, ws.vals[1], ws.vals[0],
+                                                         L.key_capacity);
+        GS_CUDA_CHECK();
+        *fine_vals = ws.vals[0];
         return GSEVT_OK;
     }
     BinParams p = make_params(f, ws);

@@ -9,9 +9,10 @@ int gs_launch_preprocess_bwd_cached(const gsevt_frame *f, const Workspace &ws, c
 int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gsevt_map_grads *grads_dev,
                              double *xi_out, cudaStream_t s,
                              bool reduce);
-int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s, bool coarse);
+int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s, bool coarse,
+                          bool *binned = nullptr);
 int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, uint32_t **fine_vals,
-                         cudaStream_t s);
+                         cudaStream_t s, bool binned);
 int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, cudaStream_t s);
 int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s);
 int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, const float *dL_dimage,
@@ -199,9 +200,10 @@ extern "C" int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *
     cudaMemsetAsync(ws.status, 0, 8, s);
     GS_CUDA_CHECK();
     if ((st = gs_launch_preprocess_fwd(f, ws, s))) return st;
-    if ((st = gs_launch_depth_order(f, ws, s, true))) return st;
+    bool binned = false;
+    if ((st = gs_launch_depth_order(f, ws, s, true, &binned))) return st;
     uint32_t *fine = nullptr;
-    if ((st = gs_launch_bin_coarse(f, ws, f->L.key_capacity, &fine, s))) return st;
+    if ((st = gs_launch_bin_coarse(f, ws, f->L.key_capacity, &fine, s, binned))) return st;
     if ((st = gs_launch_blend_fwd(f, ws, fine, s))) return st;
     if ((st = gs_launch_loss(f, ws, loss_out, s))) return st;
     if ((st = gs_launch_blend_bwd(f, ws, fine, nullptr, nullptr, nullptr, s))) return st;

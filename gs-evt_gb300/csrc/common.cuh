@@ -289,3 +289,21 @@ __device__ __forceinline__ double warp_sum_d(double v)
 
 // Prepares the cooperative sort on the current device (sort.cu); outside stream capture.
 void gs_sort_prepare();
+
+// Super-tile binning fused into the cooperative depth sort (sort.cu, batched tracker).
+struct GsCoarseBin {
+    const gsevt_view *views;
+    int num_views;
+    const int4 *bin;       // per slot {tiles touched, rect lo, rect hi, depth bits}
+    uint32_t *soffs;       // [num_views + 1] first super-tile of each view
+    uint2 *sranges;        // [super_bound] [start, end) of each super-tile's list
+    uint32_t *cvals;       // [capacity] the super-tile lists (slots)
+    uint32_t capacity;     // pair capacity (fine and coarse)
+    uint32_t super_bound;  // super-tile ids available (<= 256)
+    int enabled;
+};
+// Stable depth sort of the N_vis visible slots (count in status[5]) in dkeys/dvals, the
+// result in buffer 0.  With `bin` (super_bound <= 256) and a frame the cooperative sort
+// takes, the same launch also writes the super-tile lists, their ranges, soffs and the
+// pair counts (status[1], status[6]), and *binned is set.
+int gs_launch_depth_sort(const Workspace &ws, uint32_t capacity, const GsCoarseBin *bin, bool *binned, cudaStream_t s);

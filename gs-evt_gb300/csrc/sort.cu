@@ -250,6 +250,19 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
 // (release add, acquire loads); every wait is bounded by GS_SPIN_LIMIT polls, after which
 // the block records GSEVT_STATUS_SORT_TIMEOUT and continues.  Data written by other blocks
 // in an earlier phase is read with ld.global.cg (L2), never through a stale L1 line.
+// Optional tail of the depth sort in the batched tracker (gs_launch_depth_order with
+// coarse binning): after the last pass the same grid bins the depth-sorted slots through
+// 4x4-tile super-tiles.  Block b takes its run of sorted slots again; each warp expands its
+// 32nd of the run into (super-tile, slot) pairs, slot by slot in depth order and row-major
+// within a slot (the expansion of k_duplicate_coarse), counts them per super-tile
+// (sweep 1), and after the same table scan as a sort pass writes every pair straight to
+// its place in the super-tile-sorted list (sweep 2: the same expansion, ranked stably by
+// ballots).  That is the order of the stable sort of the depth-ordered pairs by
+// super-tile id, with no pair array, histogram or sort pass in between.  Block 0 also
+// numbers the views' super-tiles (soffs) and writes every super-tile's range; the fine
+// pair count and the coarse count land in status[1] and status[6].
+typedef GsCoarseBin CoopBin;
+
 struct CoopParams {
     uint32_t *keys[2];
     uint32_t *vals[2];
@@ -259,6 +272,7 @@ struct CoopParams {
     const uint32_t *count;  // number of keys (device word)
     uint32_t capacity;
     int passes;
+    CoopBin bin;
 };
 
 __device__ __forceinline__ void coop_arrive(uint32_t *ctr)
@@ -305,6 +319,96 @@ __device__ __forceinline__ uint32_t coop_digit_scan(uint32_t v, uint32_t *wsc)
     return base + inc - v;
 }
 
+// Stable in-warp ranking of one 8-bit id per lane (valid lanes only): the lanes with the
+// same validity and id are found with nine ballots; returns the lane's rank among them
+// plus the warp's running count for the id, which the group's first lane advances.
+__device__ __forceinline__ uint32_t coop_warp_rank(bool valid, uint32_t id, uint32_t *wcount, int lane)
+{
+    uint32_t peers = __ballot_sync(0xffffffffu, valid);
+    if (!valid) peers = ~peers;
+#pragma unroll
+    for (int bit = 0; bit < 8; ++bit) {
+        const uint32_t m = __ballot_sync(0xffffffffu, (id >> bit) & 1u);
+        peers &= ((id >> bit) & 1u) ? m : ~m;
+    }
+    const int leader = __ffs(peers) - 1;
+    uint32_t before = 0;
+    if (valid) before = wcount[id];
+    __syncwarp();
+    if (valid && lane == leader) wcount[id] = before + __popc(peers);
+    __syncwarp();
+    return before + __popc(peers & ((1u << lane) - 1u));
+}
+
+// Views the fused super-tile binning handles (their tables are staged in shared memory).
+#define COOP_MAX_VIEWS 64
+
+// The (super-tile id, slot) pairs of one warp's 32nd of a block's run of depth-sorted
+// slots, in order (slot by slot, row-major within a slot), 32 at a time: f(valid, id, slot)
+// is called by every lane for every batch.  The run's slots and tile rectangles are in
+// shared memory (s_vg, s_lo, s_hi), as are the views' slot offsets, super-tile offsets
+// and super-tile row lengths.
+template <typename F>
+__device__ __forceinline__ void coop_coarse_pairs(const uint32_t *s_vg, const uint32_t *s_lo, const uint32_t *s_hi,
+                                                  const uint32_t *s_vgoff, const uint32_t *s_soff,
+                                                  const int *s_stx, int num_views, uint32_t super_bound,
+                                                  uint32_t nb, uint32_t span, int w, int lane, F f)
+{
+    for (uint32_t g0 = 0; g0 < span; g0 += 32) {  // uniform over the warp
+        const uint32_t li = (uint32_t)w * span + g0 + (uint32_t)lane;
+        uint32_t vg = 0, c = 0;
+        int sx0 = 0, sy0 = 0, srw = 1, soff = 0, stx = 1;
+        if (g0 + (uint32_t)lane < span && li < nb) {
+            vg = s_vg[li];
+            const uint32_t lo4 = s_lo[li], hi4 = s_hi[li];
+            int lo = 0, hi = num_views - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_vgoff[mid] <= vg) lo = mid; else hi = mid - 1;
+            }
+            sx0 = (int)(lo4 & 0xffffu) / GS_SUPER;
+            sy0 = (int)(lo4 >> 16) / GS_SUPER;
+            const int sx1 = ((int)(hi4 & 0xffffu) - 1) / GS_SUPER + 1;
+            const int sy1 = ((int)(hi4 >> 16) - 1) / GS_SUPER + 1;
+            srw = sx1 - sx0;
+            c = (uint32_t)(srw * (sy1 - sy0));  // visible slots touch at least one tile
+            soff = (int)s_soff[lo];
+            stx = s_stx[lo];
+        }
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        const uint32_t ex = inc - c;
+        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+        for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+            const uint32_t k = k0 + (uint32_t)lane;
+            // owner: the largest lane s with ex_s <= k (empty slots resolve to a later lane)
+            int o = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const uint32_t e = __shfl_sync(0xffffffffu, ex, o + step);
+                if (e <= k) o += step;
+            }
+            const uint32_t qq = k - __shfl_sync(0xffffffffu, ex, o);
+            const int osx0 = __shfl_sync(0xffffffffu, sx0, o), osy0 = __shfl_sync(0xffffffffu, sy0, o);
+            const int osrw = __shfl_sync(0xffffffffu, srw, o), osoff = __shfl_sync(0xffffffffu, soff, o);
+            const int ostx = __shfl_sync(0xffffffffu, stx, o);
+            const uint32_t ovg = __shfl_sync(0xffffffffu, vg, o);
+            const bool valid = k < total;
+            uint32_t id = 0;
+            if (valid) {
+                const int y = osy0 + (int)(qq / (uint32_t)osrw), x = osx0 + (int)(qq % (uint32_t)osrw);
+                // ids past the layout's count (flagged by block 0) are clamped in range
+                id = min((uint32_t)(osoff + y * ostx + x), super_bound - 1u);
+            }
+            f(valid, id, ovg);
+        }
+    }
+}
+
 #define COOP_WARPS (GS_COOP_THREADS / 32)
 __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
 {
@@ -319,7 +423,25 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
     const int d = tid & 255, q = tid >> 8;  // digit and quarter (four threads per digit)
     const uint32_t G = gridDim.x, b = blockIdx.x;
     const uint32_t K = min(*p.count, p.capacity);
-    if (K == 0) return;  // uniform over the grid
+    if (p.bin.enabled && b == 0 && tid == 0) {
+        // super-tile numbering of the views; the fine-list cursor of the filter that follows
+        uint32_t carry = 0;
+        for (int v = 0; v < p.bin.num_views; ++v) {
+            const gsevt_view &V = p.bin.views[v];
+            p.bin.soffs[v] = carry;
+            carry += (uint32_t)(((V.tiles_x + GS_SUPER - 1) / GS_SUPER) * ((V.tiles_y + GS_SUPER - 1) / GS_SUPER));
+        }
+        p.bin.soffs[p.bin.num_views] = carry;
+        if (carry > p.bin.super_bound) atomicOr(p.status, GSEVT_STATUS_LAYOUT);
+        p.status[7] = 0u;
+    }
+    if (K == 0) {  // uniform over the grid: no slot is visible, every super-tile list is empty
+        if (p.bin.enabled && b == 0) {
+            for (uint32_t i = tid; i < p.bin.super_bound; i += GS_COOP_THREADS) p.bin.sranges[i] = make_uint2(0u, 0u);
+            if (tid == 0) p.status[6] = 0u;
+        }
+        return;
+    }
     if (K > G * (uint32_t)GS_COOP_TILE || G > GS_COOP_GP || G * COOP_WARPS < 256) {
         // the launcher sizes the grid for the capacity, so this is unreachable
         if (b == 0 && tid == 0) atomicOr(p.status, GSEVT_STATUS_KEY_OVERFLOW);
@@ -473,6 +595,132 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
             coop_wait(p.barrier, nbar * G, p.status);
         }
     }
+    if (!p.bin.enabled) return;
+    // ---- coarse binning of the sorted slots (the tail described above CoopBin) ----
+    __shared__ uint32_t s_vgoff[COOP_MAX_VIEWS], s_soff[COOP_MAX_VIEWS];
+    __shared__ int s_stx[COOP_MAX_VIEWS];
+    coop_arrive(p.barrier);
+    ++nbar;
+    for (int i = tid; i < COOP_WARPS * 256; i += GS_COOP_THREADS) (&whist[0][0])[i] = 0;
+    coop_wait(p.barrier, nbar * G, p.status);
+    const int nviews = min(p.bin.num_views, COOP_MAX_VIEWS);  // the launcher checks the count
+    if (tid < nviews) {
+        const gsevt_view &V = p.bin.views[tid];
+        s_vgoff[tid] = (uint32_t)V.vg_offset;
+        s_soff[tid] = __ldcg(p.bin.soffs + tid);
+        s_stx[tid] = (V.tiles_x + GS_SUPER - 1) / GS_SUPER;
+    }
+    // the block's run of sorted slots and their tile rectangles, into shared memory
+    // (the sort's staging buffers are free now); all loads of the run in flight together
+    uint32_t *s_vg = skeys, *s_lo = svals, *s_hi = sin;
+    const uint32_t *sorted = (p.passes & 1) ? p.vals[1] : p.vals[0];
+    uint32_t fine = 0;
+    for (uint32_t i = tid; i < nb; i += GS_COOP_THREADS) {
+        const uint32_t vg = __ldcg(sorted + t0 + i);
+        const int4 b4 = p.bin.bin[vg];
+        s_vg[i] = vg;
+        s_lo[i] = (uint32_t)b4.y;
+        s_hi[i] = (uint32_t)b4.z;
+        fine += (uint32_t)b4.x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) fine += __shfl_xor_sync(0xffffffffu, fine, o);
+    if (lane == 0 && fine) atomicAdd(p.status + 1, fine);
+    __syncthreads();
+    // sweep 1: pairs per (warp, super-tile)
+    coop_coarse_pairs(s_vg, s_lo, s_hi, s_vgoff, s_soff, s_stx, nviews, p.bin.super_bound, nb, span, w, lane,
+                      [&](bool valid, uint32_t id, uint32_t) { coop_warp_rank(valid, id, whist[w], lane); });
+    __syncthreads();
+    {
+        uint32_t s4 = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) s4 += whist[8 * q + i][d];
+        qall[q][d] = s4;
+    }
+    __syncthreads();
+    uint32_t pre = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t v = qall[i][d];
+        pre += i < q ? v : 0u;
+        tot += v;
+    }
+    {
+        uint32_t run = pre;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const uint32_t v = whist[8 * q + i][d];
+            whist[8 * q + i][d] = run;
+            run += v;
+        }
+    }
+    if (q == 0) p.cnt[(size_t)d * GS_COOP_GP + b] = tot;
+    coop_arrive(p.barrier);
+    ++nbar;
+    coop_wait(p.barrier, nbar * G, p.status);
+    {
+        const uint32_t r = b + (uint32_t)w * G;
+        if (r < 256) {
+            uint32_t *row = p.cnt + (size_t)r * GS_COOP_GP;
+            uint32_t v[GS_COOP_GP / 32];
+#pragma unroll
+            for (int c = 0; c < GS_COOP_GP / 32; ++c) {
+                const uint32_t col = (uint32_t)(c * 32 + lane);
+                v[c] = col < G ? __ldcg(row + col) : 0u;
+            }
+            uint32_t run = 0;
+#pragma unroll
+            for (int c = 0; c < GS_COOP_GP / 32; ++c) {
+                const uint32_t col = (uint32_t)(c * 32 + lane);
+                uint32_t inc = v[c];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                if (col < G) row[col] = run + inc - v[c];
+                run += __shfl_sync(0xffffffffu, inc, 31);
+            }
+            if (lane == 0) row_tot[r] = run;
+        }
+    }
+    coop_arrive(p.barrier);
+    ++nbar;
+    coop_wait(p.barrier, nbar * G, p.status);
+    uint32_t A = 0, E = 0;
+    if (tid < 256) {
+        E = __ldcg(p.cnt + (size_t)d * GS_COOP_GP + b);
+        A = __ldcg(row_tot + d);
+    }
+    const uint32_t ga = coop_digit_scan(A, wsc);
+    if (tid < 256) {
+        gbase[d] = ga + E;
+        if (b == 0) {
+            // clamped to the capacity: past it no pair is written (overflow is flagged below),
+            // and the filter must not read there
+            if ((uint32_t)d < p.bin.super_bound)
+                p.bin.sranges[d] = make_uint2(min(ga, p.bin.capacity), min(ga + A, p.bin.capacity));
+            if (d == 255) {
+                const uint32_t coarse = ga + A;
+                p.status[6] = coarse;
+                if (coarse > p.bin.capacity) atomicOr(p.status, GSEVT_STATUS_KEY_OVERFLOW);
+            }
+        }
+    }
+    if (b == 0 && tid == 0) {
+        // every block added its fine count before the last barrier
+        if (__ldcg(p.status + 1) > p.bin.capacity) atomicOr(p.status, GSEVT_STATUS_KEY_OVERFLOW);
+    }
+    __syncthreads();
+    // sweep 2: the same pairs, each written to its place in its super-tile's list
+    coop_coarse_pairs(s_vg, s_lo, s_hi, s_vgoff, s_soff, s_stx, nviews, p.bin.super_bound, nb, span, w, lane,
+                      [&](bool valid, uint32_t id, uint32_t slot) {
+                          const uint32_t r = coop_warp_rank(valid, id, whist[w], lane);
+                          if (valid) {
+                              const uint32_t pos = gbase[id] + r;
+                              if (pos < p.bin.capacity) p.bin.cvals[pos] = slot;
+                          }
+                      });
 }
 #undef COOP_WARPS
 
@@ -493,7 +741,72 @@ int coop_grid_query(int dev)
     return g >= 8 ? g : -1;
 }
 
+// Launches the cooperative sort when this device has it prepared and the capacity fits
+// its grid; returns false (nothing launched) otherwise.  *st receives the launch status.
+bool launch_coop(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
+                 int passes, const Workspace &ws, cudaStream_t s, const GsCoarseBin *bin, int *st)
+{
+    int dev = 0;
+    const int g = (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) ? g_coop_grid[dev] : -1;
+    if (g <= 0 || (uint64_t)capacity > (uint64_t)g * GS_COOP_TILE) return false;
+    cudaMemsetAsync(ws.sort_counter, 0, 4, s);
+    CoopParams cp;
+    cp.keys[0] = keys[0];
+    cp.keys[1] = keys[1];
+    cp.vals[0] = vals[0];
+    cp.vals[1] = vals[1];
+    cp.cnt = ws.sort_hist;
+    cp.barrier = ws.sort_counter;
+    cp.status = ws.status;
+    cp.count = count;
+    cp.capacity = capacity;
+    cp.passes = passes;
+    cp.bin = {};
+    if (bin && bin->super_bound >= 1 && bin->super_bound <= 256 && bin->num_views >= 1 &&
+        bin->num_views <= COOP_MAX_VIEWS) {
+        cp.bin = *bin;
+        cp.bin.enabled = 1;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)g);
+    cfg.blockDim = dim3(GS_COOP_THREADS);
+    cfg.dynamicSmemBytes = 3 * GS_COOP_TILE * 4;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    *st = GSEVT_OK;
+    if (cudaLaunchKernelEx(&cfg, k_sort_coop, cp) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        *st = GSEVT_ERR_CUDA;
+    return true;
+}
+
 }  // namespace
+
+template <typename KT>
+int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
+                     int bits, uint32_t max_keys, int kpt, const Workspace &ws, int *out_buf, cudaStream_t s,
+                     uint2 *ranges, uint32_t nranges);
+
+int gs_launch_depth_sort(const Workspace &ws, uint32_t capacity, const GsCoarseBin *bin, bool *binned, cudaStream_t s)
+{
+    *binned = false;
+    uint32_t *dk[2] = {ws.dkeys[0], ws.dkeys[1]};
+    uint32_t *dv[2] = {ws.dvals[0], ws.dvals[1]};
+    int st = 0;
+    if (capacity > 0 && launch_coop(dk, dv, ws.status + 5, capacity, 4, ws, s, bin, &st)) {
+        *binned = st == GSEVT_OK && bin && bin->super_bound >= 1 && bin->super_bound <= 256 && bin->num_views >= 1 &&
+                  bin->num_views <= COOP_MAX_VIEWS;
+        return st;
+    }
+    int buf = 0;
+    st = gs_launch_sort_t<uint32_t>(dk, dv, ws.status + 5, capacity, 32, capacity, GS_SORT_KPT_DEPTH, ws, &buf, s,
+                                    nullptr, 0);
+    if (st) return st;
+    return buf == 0 ? GSEVT_OK : GSEVT_ERR_ARG;  // 4 passes: the result is back in buffer 0
+}
 
 // Sets up the cooperative sort on the current device (function attributes and its grid);
 // called outside stream capture, e.g. when a workspace is initialised.  A sort launched
@@ -527,35 +840,8 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
     if (max_keys > capacity) max_keys = capacity;
     if (max_keys == 0) return GSEVT_OK;
     if (sizeof(KT) == 4 && passes >= 2 && !ranges) {
-        int dev = 0;
-        const int g = (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) ? g_coop_grid[dev] : -1;
-        if (g > 0 && (uint64_t)capacity <= (uint64_t)g * GS_COOP_TILE) {
-            cudaMemsetAsync(ws.sort_counter, 0, 4, s);
-            CoopParams cp;
-            cp.keys[0] = (uint32_t *)keys[0];
-            cp.keys[1] = (uint32_t *)keys[1];
-            cp.vals[0] = vals[0];
-            cp.vals[1] = vals[1];
-            cp.cnt = ws.sort_hist;
-            cp.barrier = ws.sort_counter;
-            cp.status = ws.status;
-            cp.count = count;
-            cp.capacity = capacity;
-            cp.passes = passes;
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3((unsigned)g);
-            cfg.blockDim = dim3(GS_COOP_THREADS);
-            cfg.dynamicSmemBytes = 3 * GS_COOP_TILE * 4;
-            cfg.stream = s;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeCooperative;
-            attr[0].val.cooperative = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            if (cudaLaunchKernelEx(&cfg, k_sort_coop, cp) != cudaSuccess) return GSEVT_ERR_CUDA;
-            GS_CUDA_CHECK();
-            return GSEVT_OK;
-        }
+        int st = 0;
+        if (launch_coop((uint32_t *const *)keys, vals, count, capacity, passes, ws, s, nullptr, &st)) return st;
     }
     cudaMemsetAsync(ws.sort_hist, 0, GS_MAX_PASSES * 256 * 4, s);
     cudaMemsetAsync(ws.sort_counter, 0, GS_MAX_PASSES * 4, s);
