@@ -22,7 +22,10 @@
 // k_filter_tiles cuts every tile's list out of its super-tile's group, in order.  The
 // per-tile lists equal those of steps 4-5 (gs_launch_bin_coarse).
 // With at most 256 super-tiles (the layout's super_tiles) the super-tile sort is a single
-// pass whose first block also writes the super-tile ranges (no range kernel).
+// pass whose first block also writes the super-tile ranges (no range kernel).  When the
+// depth sort runs as one cooperative launch (sort.cu), that launch also produces the
+// super-tile lists and ranges (steps 3-5 of the coarse path in the same grid), and only
+// the filter follows.
 #include "common.cuh"
 
 template <typename KT>

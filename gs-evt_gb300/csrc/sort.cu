@@ -1,4 +1,9 @@
-// Onesweep LSD radix sort of (32- or 64-bit key, 32-bit value) pairs, 8-bit digits.
+// LSD radix sorts of (32-bit key, 32-bit value) pairs, 8-bit digits, stable.
+//
+// Two implementations with identical results: a sort whose capacity fits 8192 keys per
+// SM runs all its passes in one cooperative launch (k_sort_coop, below the onesweep
+// kernels; the batched tracker's depth sort also bins the sorted slots through
+// super-tiles in that launch); larger sorts run the onesweep passes described next.
 //
 // Method: Adinets & Merrill, "Onesweep: A Faster Least Significant Digit Radix Sort
 // for GPUs" (2022).  One histogram kernel reads the keys once and counts the digits of
