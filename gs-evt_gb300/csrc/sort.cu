@@ -22,6 +22,8 @@
 // predecessor is bounded by GS_SPIN_LIMIT polls; on expiry the block records
 // GSEVT_STATUS_SORT_TIMEOUT and continues, so a fault can never hang the GPU.
 // Stability: ranks follow (warp, key slot, lane) order, which is the input order.
+#include <atomic>
+
 #include "common.cuh"
 
 namespace {
@@ -729,8 +731,10 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
 }
 #undef COOP_WARPS
 
-// grid of the cooperative sort on each device: 0 not prepared, -1 unavailable
-int g_coop_grid[64];
+// grid of the cooperative sort on each device: 0 not prepared, -1 unavailable (set once
+// per device by gs_sort_prepare, read by every launch; atomic so that workspaces set up
+// from several host threads are safe)
+std::atomic<int> g_coop_grid[64];
 
 int coop_grid_query(int dev)
 {
@@ -752,7 +756,9 @@ bool launch_coop(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_
                  int passes, const Workspace &ws, cudaStream_t s, const GsCoarseBin *bin, int *st)
 {
     int dev = 0;
-    const int g = (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) ? g_coop_grid[dev] : -1;
+    const int g = (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64)
+                      ? g_coop_grid[dev].load(std::memory_order_relaxed)
+                      : -1;
     if (g <= 0 || (uint64_t)capacity > (uint64_t)g * GS_COOP_TILE) return false;
     cudaMemsetAsync(ws.sort_counter, 0, 4, s);
     CoopParams cp;
@@ -821,7 +827,8 @@ void gs_sort_prepare()
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); return; }
-    if (g_coop_grid[dev] == 0) g_coop_grid[dev] = coop_grid_query(dev);
+    if (g_coop_grid[dev].load(std::memory_order_relaxed) == 0)
+        g_coop_grid[dev].store(coop_grid_query(dev), std::memory_order_relaxed);
     cudaGetLastError();
 }
 
