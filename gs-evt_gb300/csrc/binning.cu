@@ -564,6 +564,8 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
         cb.cvals = ws.vals[1];
         cb.capacity = (uint32_t)L.key_capacity;
         cb.super_bound = gs_super_bound(L);
+        cb.rec_a = ws.keys[0];  // the pair key buffers are free in this path
+        cb.rec_b = ws.keys[1];
         cb.enabled = 1;
     }
     bool fused = false;

@@ -300,6 +300,8 @@ struct GsCoarseBin {
     uint32_t *cvals;       // [capacity] the super-tile lists (slots)
     uint32_t capacity;     // pair capacity (fine and coarse)
     uint32_t super_bound;  // super-tile ids available (<= 256)
+    uint32_t *rec_a;       // [capacity] scratch: each pair's super-tile id and rank in its warp
+    uint32_t *rec_b;       // [capacity] scratch: each pair's slot
     int enabled;
 };
 // Stable depth sort of the N_vis visible slots (count in status[5]) in dkeys/dvals, the

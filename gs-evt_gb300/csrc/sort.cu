@@ -363,7 +363,7 @@ __device__ __forceinline__ void coop_coarse_pairs(const uint32_t *s_vg, const ui
 {
     for (uint32_t g0 = 0; g0 < span; g0 += 32) {  // uniform over the warp
         const uint32_t li = (uint32_t)w * span + g0 + (uint32_t)lane;
-        uint32_t vg = 0, c = 0;
+        uint32_t vg = 0, c = 0, mg = 0;
         int sx0 = 0, sy0 = 0, srw = 1, soff = 0, stx = 1;
         if (g0 + (uint32_t)lane < span && li < nb) {
             vg = s_vg[li];
@@ -381,6 +381,9 @@ __device__ __forceinline__ void coop_coarse_pairs(const uint32_t *s_vg, const ui
             c = (uint32_t)(srw * (sy1 - sy0));  // visible slots touch at least one tile
             soff = (int)s_soff[lo];
             stx = s_stx[lo];
+            // q / srw = umulhi(q, floor((2^32 - 1) / srw) + 1), exact for q < 2^16 and
+            // 2 <= srw <= 2^16 (here q < 256: at most 256 super-tiles)
+            mg = srw > 1 ? 0xffffffffu / (uint32_t)srw + 1u : 0u;
         }
         uint32_t inc = c;
 #pragma unroll
@@ -403,11 +406,12 @@ __device__ __forceinline__ void coop_coarse_pairs(const uint32_t *s_vg, const ui
             const int osx0 = __shfl_sync(0xffffffffu, sx0, o), osy0 = __shfl_sync(0xffffffffu, sy0, o);
             const int osrw = __shfl_sync(0xffffffffu, srw, o), osoff = __shfl_sync(0xffffffffu, soff, o);
             const int ostx = __shfl_sync(0xffffffffu, stx, o);
-            const uint32_t ovg = __shfl_sync(0xffffffffu, vg, o);
+            const uint32_t ovg = __shfl_sync(0xffffffffu, vg, o), omg = __shfl_sync(0xffffffffu, mg, o);
             const bool valid = k < total;
             uint32_t id = 0;
             if (valid) {
-                const int y = osy0 + (int)(qq / (uint32_t)osrw), x = osx0 + (int)(qq % (uint32_t)osrw);
+                const uint32_t qy = osrw > 1 ? __umulhi(qq, omg) : qq;
+                const int y = osy0 + (int)qy, x = osx0 + (int)(qq - qy * (uint32_t)osrw);
                 // ids past the layout's count (flagged by block 0) are clamped in range
                 id = min((uint32_t)(osoff + y * ostx + x), super_bound - 1u);
             }
@@ -634,9 +638,24 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
     for (int o = 16; o > 0; o >>= 1) fine += __shfl_xor_sync(0xffffffffu, fine, o);
     if (lane == 0 && fine) atomicAdd(p.status + 1, fine);
     __syncthreads();
-    // sweep 1: pairs per (warp, super-tile)
+    // sweep 1: pairs per (warp, super-tile); each pair's id, rank in its warp and slot are
+    // also recorded in the warp's share of the scratch buffers, so that sweep 2 only has to
+    // place them (a warp whose pairs overflow its share expands them again instead)
+    __shared__ uint32_t s_nw[COOP_WARPS];
+    const uint32_t rw_cap = p.bin.capacity / G / COOP_WARPS;
+    const size_t rbase = ((size_t)b * COOP_WARPS + (size_t)w) * rw_cap;
+    uint32_t nrec = 0;
     coop_coarse_pairs(s_vg, s_lo, s_hi, s_vgoff, s_soff, s_stx, nviews, p.bin.super_bound, nb, span, w, lane,
-                      [&](bool valid, uint32_t id, uint32_t) { coop_warp_rank(valid, id, whist[w], lane); });
+                      [&](bool valid, uint32_t id, uint32_t slot) {
+                          const uint32_t r = coop_warp_rank(valid, id, whist[w], lane);
+                          const uint32_t j = nrec + (uint32_t)lane;  // valid lanes are a prefix
+                          if (valid && j < rw_cap) {
+                              p.bin.rec_a[rbase + j] = (id << 24) | r;
+                              p.bin.rec_b[rbase + j] = slot;
+                          }
+                          nrec += __popc(__ballot_sync(0xffffffffu, valid));
+                      });
+    if (lane == 0) s_nw[w] = nrec;
     __syncthreads();
     {
         uint32_t s4 = 0;
@@ -719,15 +738,26 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
         if (__ldcg(p.status + 1) > p.bin.capacity) atomicOr(p.status, GSEVT_STATUS_KEY_OVERFLOW);
     }
     __syncthreads();
-    // sweep 2: the same pairs, each written to its place in its super-tile's list
-    coop_coarse_pairs(s_vg, s_lo, s_hi, s_vgoff, s_soff, s_stx, nviews, p.bin.super_bound, nb, span, w, lane,
-                      [&](bool valid, uint32_t id, uint32_t slot) {
-                          const uint32_t r = coop_warp_rank(valid, id, whist[w], lane);
-                          if (valid) {
-                              const uint32_t pos = gbase[id] + r;
-                              if (pos < p.bin.capacity) p.bin.cvals[pos] = slot;
-                          }
-                      });
+    // sweep 2: every pair to its place in its super-tile's list (gbase: the super-tile's
+    // start plus the pairs of earlier blocks; whist: the pairs of earlier warps of the block)
+    const uint32_t nw = s_nw[w];  // uniform over the warp
+    if (nw <= rw_cap) {
+        for (uint32_t j = (uint32_t)lane; j < nw; j += 32) {
+            const uint32_t a = __ldcg(p.bin.rec_a + rbase + j), slot = __ldcg(p.bin.rec_b + rbase + j);
+            const uint32_t id = a >> 24;
+            const uint32_t pos = gbase[id] + whist[w][id] + (a & 0xffffffu);
+            if (pos < p.bin.capacity) p.bin.cvals[pos] = slot;
+        }
+    } else {
+        coop_coarse_pairs(s_vg, s_lo, s_hi, s_vgoff, s_soff, s_stx, nviews, p.bin.super_bound, nb, span, w, lane,
+                          [&](bool valid, uint32_t id, uint32_t slot) {
+                              const uint32_t r = coop_warp_rank(valid, id, whist[w], lane);
+                              if (valid) {
+                                  const uint32_t pos = gbase[id] + r;
+                                  if (pos < p.bin.capacity) p.bin.cvals[pos] = slot;
+                              }
+                          });
+    }
 }
 #undef COOP_WARPS
 
