@@ -46,6 +46,9 @@ def test_workspace_sizing_and_offsets():
     assert off["status"] == 0 and off["recC"] is None and off["gradC"] is None
     seen = [v for v in off.values() if v is not None]
     assert seen == sorted(seen) and all(v % 256 == 0 for v in seen)
+    # the sort-count region also holds the cooperative sort's digit-major table:
+    # 256 digits x 160 block columns plus 256 row totals, 32-bit each
+    assert off["sort_counter"] - off["sort_hist"] >= (160 + 1) * 256 * 4
 
 
 def test_argument_validation_without_gpu():
