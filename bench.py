@@ -591,22 +591,24 @@ def main():
             traffic = json.load(open(tpath)).get(args.workload, {}).get(top)
         except Exception:
             traffic = None
-    # kernels per iteration of the batched step: preprocess, visible scan, compaction,
-    # then either one cooperative launch (visible-slot capacity within 8192 keys per SM
-    # and at most 256 super-tiles) that sorts by depth and builds the super-tile lists,
-    # or the depth sort (cooperative, or a histogram and 4 onesweep passes), sorted sums,
-    # paired scan, coarse duplication and the super-tile sort (histogram, passes, + a
-    # range kernel when there are two); then tile filter, blend fwd, loss, blend bwd,
-    # preprocess bwd, finalize
+    # kernels per iteration of the batched step: preprocess, visible scan and compaction
+    # (inside the cooperative sort when it runs), then either one cooperative launch
+    # (visible-slot capacity within 8192 keys per SM and at most 256 super-tiles) that
+    # sorts by depth and builds the super-tile lists, or the depth sort (cooperative, or a
+    # histogram and 4 onesweep passes), sorted sums, paired scan, coarse duplication and
+    # the super-tile sort (histogram, passes, + a range kernel when there are two); then
+    # tile filter, blend fwd, loss, blend bwd, preprocess bwd, finalize
     L = bt.frame.L
     nsup = L.super_tiles if L.super_tiles > 0 else L.total_tiles // 4 + L.num_views + 1
     super_passes = (max(1, int(nsup - 1).bit_length()) + 7) // 8
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    coop = L.num_vg <= min(sms, 160) * 8192
+    coop_keys = min(sms, 160) * 8192
+    coop = L.num_vg <= coop_keys
+    compact_launches = 0 if coop and L.num_scan_blocks * 256 <= coop_keys else 2
     if coop and super_passes == 1:
-        launches_per_iter = 10
+        launches_per_iter = 8 + compact_launches
     else:
-        launches_per_iter = 13 + (1 if coop else 5) + super_passes + (1 if super_passes > 1 else 0)
+        launches_per_iter = 11 + compact_launches + (1 if coop else 5) + super_passes + (1 if super_passes > 1 else 0)
     it_bytes = iteration_bytes(prob, dev)
     it_gbs = it_bytes["bytes_per_iter"] * (1000.0 / ms) / 1e9
     line = {

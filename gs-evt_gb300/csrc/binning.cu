@@ -551,9 +551,25 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
         return GSEVT_OK;
     }
     BinParams p = make_params(f, ws);
-    k_scan_blocks<<<1, 1024, 0, s>>>(ws.vis_sums, ws.vis_offs, L.num_scan_blocks, ws.status + 5, ws.status, 0);
-    k_compact<<<L.num_scan_blocks, GS_BLOCK, 0, s>>>(p);
-    GS_CUDA_CHECK();
+    // the cooperative sort compacts the visible slots in its first pass; otherwise the
+    // visible-slot scan and compaction kernels run first
+    GsCompact cmp = {};
+    const bool fuse_compact = gs_coop_depth_sort((uint32_t)L.num_vg, (uint32_t)L.num_scan_blocks);
+    if (fuse_compact) {
+        cmp.views = f->views;
+        cmp.num_views = L.num_views;
+        cmp.maps = f->maps;
+        cmp.bin = ws.bin;
+        cmp.gradA = ws.gradA;
+        cmp.gradB = ws.gradB;
+        cmp.gradC = L.channels == 3 ? ws.gradC : nullptr;
+        cmp.num_scan_blocks = (uint32_t)L.num_scan_blocks;
+        cmp.enabled = 1;
+    } else {
+        k_scan_blocks<<<1, 1024, 0, s>>>(ws.vis_sums, ws.vis_offs, L.num_scan_blocks, ws.status + 5, ws.status, 0);
+        k_compact<<<L.num_scan_blocks, GS_BLOCK, 0, s>>>(p);
+        GS_CUDA_CHECK();
+    }
     GsCoarseBin cb = {};
     if (coarse && binned && gs_super_bits(L) <= 8 && L.total_tiles > 0) {
         cb.views = f->views;
@@ -569,7 +585,8 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
         cb.enabled = 1;
     }
     bool fused = false;
-    int st = gs_launch_depth_sort(ws, (uint32_t)L.num_vg, cb.enabled ? &cb : nullptr, &fused, s);
+    int st = gs_launch_depth_sort(ws, (uint32_t)L.num_vg, fuse_compact ? &cmp : nullptr, cb.enabled ? &cb : nullptr,
+                                  &fused, s);
     if (st) return st;
     if (fused) {
         *binned = true;

@@ -304,8 +304,25 @@ struct GsCoarseBin {
     uint32_t *rec_b;       // [capacity] scratch: each pair's slot
     int enabled;
 };
+// Visible-slot compaction fused into the first pass of the cooperative depth sort: the
+// pass reads every (view, Gaussian) slot's bin record itself, keeps the visible ones in
+// slot order, clears their gradient records and writes N_vis to status[5].
+struct GsCompact {
+    const gsevt_view *views;
+    int num_views;
+    const gsevt_map *maps;
+    const int4 *bin;
+    float4 *gradA, *gradB, *gradC;  // gradC null without RGB
+    uint32_t num_scan_blocks;
+    int enabled;
+};
+// True when the cooperative sort runs a depth sort of this capacity on the current device
+// (and, for the compaction, of this many scan blocks).
+bool gs_coop_depth_sort(uint32_t capacity, uint32_t num_scan_blocks);
 // Stable depth sort of the N_vis visible slots (count in status[5]) in dkeys/dvals, the
-// result in buffer 0.  With `bin` (super_bound <= 256) and a frame the cooperative sort
+// result in buffer 0.  With `cmp` (only when gs_coop_depth_sort holds) the launch also
+// compacts the visible slots itself.  With `bin` (super_bound <= 256) and a frame the cooperative sort
 // takes, the same launch also writes the super-tile lists, their ranges, soffs and the
 // pair counts (status[1], status[6]), and *binned is set.
-int gs_launch_depth_sort(const Workspace &ws, uint32_t capacity, const GsCoarseBin *bin, bool *binned, cudaStream_t s);
+int gs_launch_depth_sort(const Workspace &ws, uint32_t capacity, const GsCompact *cmp, const GsCoarseBin *bin,
+                         bool *binned, cudaStream_t s);

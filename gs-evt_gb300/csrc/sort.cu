@@ -280,6 +280,7 @@ struct CoopParams {
     uint32_t capacity;
     int passes;
     CoopBin bin;
+    GsCompact cmp;
 };
 
 __device__ __forceinline__ void coop_arrive(uint32_t *ctr)
@@ -433,7 +434,8 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int d = tid & 255, q = tid >> 8;  // digit and quarter (four threads per digit)
     const uint32_t G = gridDim.x, b = blockIdx.x;
-    const uint32_t K = min(*p.count, p.capacity);
+    // with the compaction fused into pass 0 the key count is only known after that pass
+    uint32_t K = p.cmp.enabled ? 1u : min(*p.count, p.capacity);
     if (p.bin.enabled && b == 0 && tid == 0) {
         // super-tile numbering of the views; the fine-list cursor of the filter that follows
         uint32_t carry = 0;
@@ -459,14 +461,26 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
         return;
     }
     uint32_t *row_tot = p.cnt + 256 * GS_COOP_GP;
-    const uint32_t TS = (K + G - 1) / G;
-    const uint32_t t0 = min(K, b * TS);
-    const uint32_t nb = min(K, t0 + TS) - t0;                  // keys of this block (<= GS_COOP_TILE)
-    const uint32_t span = (nb + COOP_WARPS - 1) / COOP_WARPS;  // keys of each warp (<= 32 GS_COOP_KPT)
-    const int rounds = (int)((span + 31) / 32);
+    __shared__ uint32_t s_total[2];
+    // this block's run of keys: [t0, t0 + nb), nb <= GS_COOP_TILE; with the compaction in
+    // pass 0, that pass's run is instead scan blocks [sb0, sb0 + nsb) of the slot space
+    // (256 slots each, at most GS_COOP_TILE), of which the visible ones are its keys
+    uint32_t TS = (K + G - 1) / G;
+    uint32_t t0 = min(K, b * TS);
+    uint32_t nb = min(K, t0 + TS) - t0;
+    uint32_t sb0 = 0;
+    if (p.cmp.enabled) {
+        const uint32_t per = (p.cmp.num_scan_blocks + G - 1) / G;
+        sb0 = min(p.cmp.num_scan_blocks, b * per);
+        nb = (min(p.cmp.num_scan_blocks, sb0 + per) - sb0) * (uint32_t)GS_BLOCK;
+        t0 = 0;
+    }
+    uint32_t span = (nb + COOP_WARPS - 1) / COOP_WARPS;  // keys of each warp (<= 32 GS_COOP_KPT)
+    int rounds = (int)((span + 31) / 32);
     const uint32_t lt = (1u << lane) - 1u;
     uint32_t nbar = 0;
     for (int pass = 0; pass < p.passes; ++pass) {
+        const bool compact = p.cmp.enabled && pass == 0;  // uniform
         const bool odd = (pass & 1) != 0;  // selects, not a dynamic index into the parameters
         const uint32_t *kin = odd ? p.keys[1] : p.keys[0], *vin = odd ? p.vals[1] : p.vals[0];
         uint32_t *kout = odd ? p.keys[0] : p.keys[1], *vout = odd ? p.vals[0] : p.vals[1];
@@ -475,14 +489,50 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
         // keys into registers, values staged in shared memory in input order
         uint32_t key[GS_COOP_KPT], rank[GS_COOP_KPT];
         uint32_t ok = 0;
+        if (compact) {
+            // slot li of the run: scan block sb0 + li / 256, thread li % 256 of it; a key
+            // when the slot exists and touches a tile (the visibility test of k_compact)
 #pragma unroll
-        for (int k = 0; k < GS_COOP_KPT; ++k) {
-            const uint32_t o = (uint32_t)(k * 32 + lane), li = (uint32_t)w * span + o;
-            const bool v = o < span && li < nb;
-            key[k] = v ? __ldcg(kin + t0 + li) : 0u;
-            if (v) sin[li] = __ldcg(vin + t0 + li);
-            rank[k] = 0u;
-            ok |= (uint32_t)v << k;
+            for (int k = 0; k < GS_COOP_KPT; ++k) {
+                const uint32_t o = (uint32_t)(k * 32 + lane), li = (uint32_t)w * span + o;
+                bool v = false;
+                key[k] = 0u;
+                rank[k] = 0u;
+                if (o < span && li < nb) {
+                    const int sb = (int)(sb0 + li / GS_BLOCK);
+                    int lo = 0, hi = p.cmp.num_views - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (p.cmp.views[mid].sb_offset <= sb) lo = mid; else hi = mid - 1;
+                    }
+                    const gsevt_view &V = p.cmp.views[lo];
+                    const int g = (sb - V.sb_offset) * GS_BLOCK + (int)(li % GS_BLOCK);
+                    if (g < p.cmp.maps[V.map].n) {
+                        const uint32_t vg = (uint32_t)V.vg_offset + (uint32_t)g;
+                        const int4 b4 = p.cmp.bin[vg];
+                        if (b4.x > 0) {
+                            v = true;
+                            key[k] = (uint32_t)b4.w;
+                            sin[li] = vg;
+                            // the adjoint blend accumulates into these with atomics
+                            p.cmp.gradA[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            p.cmp.gradB[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            if (p.cmp.gradC) p.cmp.gradC[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        }
+                    }
+                }
+                ok |= (uint32_t)v << k;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < GS_COOP_KPT; ++k) {
+                const uint32_t o = (uint32_t)(k * 32 + lane), li = (uint32_t)w * span + o;
+                const bool v = o < span && li < nb;
+                key[k] = v ? __ldcg(kin + t0 + li) : 0u;
+                if (v) sin[li] = __ldcg(vin + t0 + li);
+                rank[k] = 0u;
+                ok |= (uint32_t)v << k;
+            }
         }
         __syncthreads();
         // stable ranks within each warp's keys, per-warp digit counts
@@ -541,6 +591,7 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
         {
             const uint32_t ds = coop_digit_scan(tot, wsc);
             if (tid < 256) dstart[d] = ds;
+            if (tid == 255) s_total[0] = ds + tot;  // this block's keys
         }
         __syncthreads();
 #pragma unroll
@@ -592,19 +643,38 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
         {
             const uint32_t ga = coop_digit_scan(A, wsc);
             if (tid < 256) gbase[d] = ga + E;
+            if (tid == 255) s_total[1] = ga + A;  // all blocks' keys
         }
         __syncthreads();
-        for (uint32_t i = tid; i < nb; i += GS_COOP_THREADS) {
+        const uint32_t nwrite = s_total[0];
+        for (uint32_t i = tid; i < nwrite; i += GS_COOP_THREADS) {
             const uint32_t kk = skeys[i];
             const uint32_t dg = (kk >> shift) & 255u;
             kout[gbase[dg] + (i - dstart[dg])] = kk;
             vout[gbase[dg] + (i - dstart[dg])] = svals[i];
+        }
+        if (compact) {
+            // the visible slots are now keys [0, K) of buffer 1: the runs of the later passes
+            K = s_total[1];
+            if (b == 0 && tid == 0) p.status[5] = K;  // N_vis
+            TS = (K + G - 1) / G;
+            t0 = min(K, b * TS);
+            nb = min(K, t0 + TS) - t0;
+            span = (nb + COOP_WARPS - 1) / COOP_WARPS;
+            rounds = (int)((span + 31) / 32);
         }
         if (pass + 1 < p.passes) {
             coop_arrive(p.barrier);
             ++nbar;
             coop_wait(p.barrier, nbar * G, p.status);
         }
+    }
+    if (K == 0) {  // no visible slot (uniform; only reachable with the compaction in pass 0)
+        if (p.bin.enabled && b == 0) {
+            for (uint32_t i = tid; i < p.bin.super_bound; i += GS_COOP_THREADS) p.bin.sranges[i] = make_uint2(0u, 0u);
+            if (tid == 0) p.status[6] = 0u;
+        }
+        return;
     }
     if (!p.bin.enabled) return;
     // ---- coarse binning of the sorted slots (the tail described above CoopBin) ----
@@ -782,14 +852,20 @@ int coop_grid_query(int dev)
 
 // Launches the cooperative sort when this device has it prepared and the capacity fits
 // its grid; returns false (nothing launched) otherwise.  *st receives the launch status.
-bool launch_coop(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
-                 int passes, const Workspace &ws, cudaStream_t s, const GsCoarseBin *bin, int *st)
+int coop_grid_here()
 {
     int dev = 0;
-    const int g = (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64)
-                      ? g_coop_grid[dev].load(std::memory_order_relaxed)
-                      : -1;
+    return (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) ? g_coop_grid[dev].load(std::memory_order_relaxed)
+                                                                        : -1;
+}
+
+bool launch_coop(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_t *count, uint32_t capacity,
+                 int passes, const Workspace &ws, cudaStream_t s, const GsCoarseBin *bin, int *st,
+                 const GsCompact *cmp = nullptr)
+{
+    const int g = coop_grid_here();
     if (g <= 0 || (uint64_t)capacity > (uint64_t)g * GS_COOP_TILE) return false;
+    if (cmp && (uint64_t)cmp->num_scan_blocks * GS_BLOCK > (uint64_t)g * GS_COOP_TILE) return false;
     cudaMemsetAsync(ws.sort_counter, 0, 4, s);
     CoopParams cp;
     cp.keys[0] = keys[0];
@@ -802,6 +878,11 @@ bool launch_coop(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_
     cp.count = count;
     cp.capacity = capacity;
     cp.passes = passes;
+    cp.cmp = {};
+    if (cmp) {
+        cp.cmp = *cmp;
+        cp.cmp.enabled = 1;
+    }
     cp.bin = {};
     if (bin && bin->super_bound >= 1 && bin->super_bound <= 256 && bin->num_views >= 1 &&
         bin->num_views <= COOP_MAX_VIEWS) {
@@ -831,17 +912,26 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
                      int bits, uint32_t max_keys, int kpt, const Workspace &ws, int *out_buf, cudaStream_t s,
                      uint2 *ranges, uint32_t nranges);
 
-int gs_launch_depth_sort(const Workspace &ws, uint32_t capacity, const GsCoarseBin *bin, bool *binned, cudaStream_t s)
+bool gs_coop_depth_sort(uint32_t capacity, uint32_t num_scan_blocks)
+{
+    const int g = coop_grid_here();
+    return g > 0 && capacity > 0 && (uint64_t)capacity <= (uint64_t)g * GS_COOP_TILE &&
+           (uint64_t)num_scan_blocks * GS_BLOCK <= (uint64_t)g * GS_COOP_TILE;
+}
+
+int gs_launch_depth_sort(const Workspace &ws, uint32_t capacity, const GsCompact *cmp, const GsCoarseBin *bin,
+                         bool *binned, cudaStream_t s)
 {
     *binned = false;
     uint32_t *dk[2] = {ws.dkeys[0], ws.dkeys[1]};
     uint32_t *dv[2] = {ws.dvals[0], ws.dvals[1]};
     int st = 0;
-    if (capacity > 0 && launch_coop(dk, dv, ws.status + 5, capacity, 4, ws, s, bin, &st)) {
+    if (capacity > 0 && launch_coop(dk, dv, ws.status + 5, capacity, 4, ws, s, bin, &st, cmp)) {
         *binned = st == GSEVT_OK && bin && bin->super_bound >= 1 && bin->super_bound <= 256 && bin->num_views >= 1 &&
                   bin->num_views <= COOP_MAX_VIEWS;
         return st;
     }
+    if (cmp) return GSEVT_ERR_ARG;  // the compaction runs only inside the cooperative sort
     int buf = 0;
     st = gs_launch_sort_t<uint32_t>(dk, dv, ws.status + 5, capacity, 32, capacity, GS_SORT_KPT_DEPTH, ws, &buf, s,
                                     nullptr, 0);
