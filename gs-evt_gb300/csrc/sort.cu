@@ -239,7 +239,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
 // Sorts of at most G x GS_COOP_TILE keys with two or more passes run every pass in one
 // cooperative launch of G = (SMs x resident blocks) 1024-thread blocks.  Block b owns the
 // contiguous run [b TS, (b + 1) TS) of the keys, TS = ceil(K / G), the same run in every
-// pass.  A pass:
+// pass (for the depth sort with the compaction in pass 0, that pass's run is a range of
+// 256-slot scan blocks instead, of which the visible slots are the keys).  A pass:
 //   1. the block ranks its run stably (warp w takes the w-th 32nd of the run in rounds of
 //      32 keys; the lanes holding the same digit are found with nine ballots, so ranks
 //      follow the input order) and writes its 256 digit counts into column b of a
@@ -261,11 +262,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
 // coarse binning): after the last pass the same grid bins the depth-sorted slots through
 // 4x4-tile super-tiles.  Block b takes its run of sorted slots again; each warp expands its
 // 32nd of the run into (super-tile, slot) pairs, slot by slot in depth order and row-major
-// within a slot (the expansion of k_duplicate_coarse), counts them per super-tile
-// (sweep 1), and after the same table scan as a sort pass writes every pair straight to
-// its place in the super-tile-sorted list (sweep 2: the same expansion, ranked stably by
-// ballots).  That is the order of the stable sort of the depth-ordered pairs by
-// super-tile id, with no pair array, histogram or sort pass in between.  Block 0 also
+// within a slot (the expansion of k_duplicate_coarse), ranks them stably per super-tile
+// with ballots and records each pair's id, rank and slot (sweep 1); after the same table
+// scan as a sort pass it writes every recorded pair straight to its place in the
+// super-tile-sorted list (sweep 2; a warp whose records overflowed its share of the
+// scratch expands its pairs again).  That is the order of the stable sort of the
+// depth-ordered pairs by super-tile id, with no histogram or sort pass in between.  Block 0 also
 // numbers the views' super-tiles (soffs) and writes every super-tile's range; the fine
 // pair count and the coarse count land in status[1] and status[6].
 typedef GsCoarseBin CoopBin;
