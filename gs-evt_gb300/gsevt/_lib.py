@@ -23,6 +23,18 @@ STATUS_KEY_OVERFLOW = 1
 STATUS_SORT_TIMEOUT = 2
 STATUS_NONFINITE = 4
 STATUS_LAYOUT = 8
+_STATUS_NAMES = ((STATUS_KEY_OVERFLOW, "key capacity overflow"), (STATUS_SORT_TIMEOUT, "bounded device wait ran out"),
+                 (STATUS_NONFINITE, "non-finite loss or gradient"),
+                 (STATUS_LAYOUT, "layout provides too few super-tiles"))
+
+
+def status_names(flags):
+    """The conditions set in a device status word (gsevt_read_status word 0), as text."""
+    names = [n for bit, n in _STATUS_NAMES if flags & bit]
+    rest = flags & ~sum(bit for bit, _ in _STATUS_NAMES)
+    if rest:
+        names.append("unknown flags %#x" % rest)
+    return ", ".join(names) if names else "none"
 TILE = 16
 MAP_PLANES = 15
 LOSS_PIXELS_PER_BLOCK = 2048

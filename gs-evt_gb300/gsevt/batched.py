@@ -335,8 +335,9 @@ class BatchedSequenceTracker:
                 st_b = self._host_states()
                 host = (_lib.PoseState * n).from_buffer_copy(st_b.tobytes())
                 stat, _ = tr.frame.status()
-                if stat & _lib.STATUS_KEY_OVERFLOW:
-                    raise RuntimeError("key capacity overflow at pyramid level %d" % lvl)
+                bad = stat & (_lib.STATUS_KEY_OVERFLOW | _lib.STATUS_SORT_TIMEOUT | _lib.STATUS_LAYOUT)
+                if bad:
+                    raise RuntimeError("tracking at pyramid level %d: %s" % (lvl, _lib.status_names(bad)))
             self.fitted = True
             for slot, pi in enumerate(self.order):
                 s = host[slot]

@@ -62,3 +62,11 @@ def test_argument_validation_without_gpu():
                                      None, None) == -1  # even kernel size
     assert L.gsevt_pack_map(10, None, None, None, None, None, None, 16, 1.0, None, None) == -1
     assert L.gsevt_chain_view_grad(None, None, 0.0, None, None, None, None) == -1
+
+
+def test_status_names():
+    assert _lib.status_names(0) == "none"
+    assert _lib.status_names(_lib.STATUS_KEY_OVERFLOW | _lib.STATUS_LAYOUT) == (
+        "key capacity overflow, layout provides too few super-tiles")
+    assert _lib.status_names(_lib.STATUS_SORT_TIMEOUT) == "bounded device wait ran out"
+    assert "unknown flags 0x40" in _lib.status_names(0x40 | _lib.STATUS_NONFINITE)
