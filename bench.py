@@ -64,17 +64,62 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """SM clock and clock-event reasons sampled DURING the timed region (read-only).
+
+    A thread polls NVML through ctypes (libnvidia-ml.so.1, which ships with the driver)
+    every 2 ms, so that even a region of a few tens of milliseconds gets many samples;
+    without NVML it falls back to `nvidia-smi --query-gpu ... -lms 200`."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    REASONS = ((0x8, "hw_slowdown"), (0x40, "hw_thermal_slowdown"), (0x20, "sw_thermal_slowdown"),
+               (0x4, "sw_power_cap"), (0x80, "hw_power_brake_slowdown"))
 
-    def __init__(self, gpu_index=0):
-        self.gpu_index = gpu_index
+    def __init__(self, gpu_index=0, uuid=None):
+        self.gpu_index, self.uuid = gpu_index, uuid
         self.proc = None
+        self.thread = None
+        self.samples = []
+        self.stop_flag = threading.Event()
+
+    def _nvml(self):
+        import ctypes as C
+        nv = C.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            return None
+        h = C.c_void_p()
+        ok = False
+        if self.uuid:
+            ok = nv.nvmlDeviceGetHandleByUUID(self.uuid.encode(), C.byref(h)) == 0
+        if not ok:
+            ok = nv.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.gpu_index), C.byref(h)) == 0
+        return (nv, h) if ok else None
 
     def start(self):
+        try:
+            handle = self._nvml()
+        except Exception:
+            handle = None
+        if handle is not None:
+            import ctypes as C
+            nv, h = handle
+            mx = C.c_uint(0)
+            nv.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx))
+            self.max_mhz = float(mx.value)
+
+            def run():
+                clk, rs = C.c_uint(0), C.c_ulonglong(0)
+                while not self.stop_flag.is_set():
+                    if nv.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0 and \
+                            nv.nvmlDeviceGetCurrentClocksEventReasons(h, C.byref(rs)) == 0:
+                        self.samples.append((float(clk.value), int(rs.value)))
+                    time.sleep(0.002)
+
+            self.thread = threading.Thread(target=run, daemon=True)
+            self.thread.start()
+            return
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu_index), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -83,6 +128,14 @@ class ClockSampler:
             self.proc = None
 
     def stop(self):
+        if self.thread is not None:
+            self.stop_flag.set()
+            self.thread.join()
+            if not self.samples:
+                return None
+            reasons = sorted({nm for _, r in self.samples for bit, nm in self.REASONS if r & bit})
+            return {"sm_mhz": statistics.median(c for c, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                    "reasons": reasons, "samples": len(self.samples), "source": "nvml, 2 ms"}
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -108,7 +161,17 @@ class ClockSampler:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, 200 ms"}
+
+
+def gpu_uuid(dev):
+    """NVML-style UUID string of a torch device (None when torch does not expose it)."""
+    import torch
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        return None
 
 
 def build_problem(name, device, seed_offset=0):
@@ -233,6 +296,90 @@ def run_sequences(dev, flush, steps=10, warmup=3, count=16):
     return {"workload": "sequences-16-uneven", "problems": count, "views": 2 * count, "gaussians_total": total,
             "ms_per_iter": ms, "problem_iters_per_s": 1000.0 / ms * count, "keys": int(bt.num_keys),
             "resolutions": ["%dx%d" % r for r in res], "l2": "flushed (256 MB write) between timed iterations"}
+
+
+def run_sequence_tracking(dev, frames=10, count=16, window_s=0.025):
+    """16 concurrent sequences tracked frame by frame along their own smooth trajectories:
+    maps of 50k-1.5M Gaussians (log-uniform, seeds 10-25), sensors 346x260 / 640x480 /
+    1280x720 in turn, event windows of 10k-2M events (log-uniform), ground-truth motion
+    T(tau) = exp(sin(2 pi 0.2 tau) [0.5 m u, 20 deg k]) (synthetic.SinusoidTrajectory),
+    `frames` consecutive windows of `window_s` each.  The events of every window are drawn
+    on the device from grey renders at the window's two end poses (not timed).  Timed:
+    BatchedSequenceTracker.track over all frames (per frame: constant-velocity prediction,
+    event pyramid, three pyramid levels of coarse / fine Adam stages with slope
+    convergence, all sequences in lockstep, weighted velocity after five frames).
+    Reports tracked frames/s over all sequences and the RMS drift against the trajectory
+    at the window centres."""
+    import torch
+    from gsevt import synthetic
+    from gsevt import pose as gpose
+    from gsevt.batched import BatchedSequenceTracker
+    from gsevt.engine import GSFrame, MapSpec, ViewSpec, pack_map
+    rng = np.random.default_rng(10)
+    res = [(346, 260), (640, 480), (1280, 720)]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(77)
+    maps, cams, trajs, counts = [], [], [], []
+    windows = [[None] * count for _ in range(frames)]
+    us = int(round(window_s * 1e6))
+    total = 0
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(5e4), np.log(1.5e6))))
+        W, H = res[i % 3]
+        f = 600.0 * W / 640.0
+        ne = int(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        m = synthetic.make_map(n, 10 + i)
+        pk = pack_map(t(m["xyz"]), t(m["opacity"]), t(m["sh"]), scales=t(m["scale"]), rotations=t(m["rot"]))
+        maps.append({"packed": pk, "n": n})
+        cams.append((i, W, H, f, f))
+        tr = synthetic.SinusoidTrajectory(10 + i)
+        trajs.append(tr)
+        counts.append(ne)
+        total += n
+        cam = synthetic.PinholeCamera(W, H, f)
+        R0, t0 = tr.pose(0.0)
+        views = [ViewSpec(W, H, 0, R=R0, t=t0, P=cam.proj, campos=gpose.campos(R0, t0), tanfovx=cam.tanfovx,
+                          tanfovy=cam.tanfovy) for _ in range(2)]
+        fr = GSFrame([MapSpec(n, packed=pk)], views, channels=1, device=dev)
+        for k in range(frames):
+            for j, tau in enumerate((k * window_s, (k + 1) * window_s)):
+                fr.set_view_pose(j, *tr.pose(tau))
+            fr.render(exact_keys=True)
+            x, y, p = synthetic.synth_events_device(fr.pixels(0)[0], fr.pixels(1)[0], ne, gen)
+            windows[k][i] = (x, y, p, np.array([k * us, (k + 1) * us], np.int64), None)
+        del fr
+    init = []
+    for tr in trajs:
+        R, tt = tr.pose(0.5 * window_s)
+        lv, av = tr.velocity(0.5 * window_s)
+        init.append((R, tt, lv, av))
+    seq = BatchedSequenceTracker(maps, cams, device=dev)
+    torch.cuda.synchronize()
+    t_start = time.perf_counter()
+    traj = seq.track(init, windows)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_start
+    drift_t, drift_r, final_t = [], [], []
+    for i, tr in enumerate(trajs):
+        et, er = [], []
+        for k, (stamp, R, tt) in enumerate(traj[i]):
+            Rg, tg = tr.pose((k + 0.5) * window_s)
+            # camera centres (world frame) and relative rotation
+            et.append(float(np.linalg.norm(gpose.campos(R, tt) - gpose.campos(Rg, tg))))
+            er.append(gpose.rotation_error_deg(R, Rg))
+        drift_t.append(float(np.sqrt(np.mean(np.square(et)))))
+        drift_r.append(float(np.sqrt(np.mean(np.square(er)))))
+        final_t.append(et[-1])
+    return {"workload": "sequences-16-uneven-tracking", "sequences": count, "frames": frames,
+            "window_s": window_s, "gaussians_total": total, "events_per_window": counts,
+            "resolutions": ["%dx%d" % r for r in res], "wall_s": wall,
+            "tracked_frames_per_s": count * frames / wall, "adam_iterations": int(seq.iterations),
+            "problem_iterations": int(sum(seq.problem_iterations)),
+            "rms_drift_mm": [1e3 * v for v in drift_t], "rms_drift_deg": drift_r,
+            "mean_rms_drift_mm": 1e3 * float(np.mean(drift_t)), "mean_rms_drift_deg": float(np.mean(drift_r)),
+            "final_error_mm": [1e3 * v for v in final_t],
+            "trajectory": "T(tau) = exp(sin(2 pi 0.2 tau) [0.5 m u, 20 deg k]), u, k unit axes per sequence"}
 
 
 def stage_times(bt, reps=5):
@@ -537,7 +684,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the 64-hypothesis and 16-sequence workloads reported beside the headline")
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
+    ap.add_argument("--sequence-frames", type=int, default=10,
+                    help="frames each of the 16 sequences tracks in the sequence-tracking workload")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "sequence-tracking"],
                     help="profile: build the workload, then run warmup + steps un-graphed iterations "
                          "(for ncu launch lists; prints no timings)")
     args = ap.parse_args()
@@ -545,6 +694,11 @@ def main():
         return run_reference(args)
     if args.mode == "profile":
         return run_profile(args)
+    if args.mode == "sequence-tracking":
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(run_sequence_tracking(torch.device("cuda", 0), frames=args.sequence_frames)))
+        return
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -569,7 +723,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, gpu_uuid(dev))
     clocks.start()
     times = time_batched(bt, args.steps, warmup, flush)
     clk = clocks.stop()
@@ -584,13 +738,9 @@ def main():
     # CUDA-event timing of the dominant stage (its own launch stream), bytes / time
     top_ms = stages[top]
     achieved = algo[top] / (top_ms * 1e-3) / 1e9
+    # DRAM traffic needs an ncu capture, which is never taken inside a timed run: null here
+    # (the per-launch traffic of the captured build is in the profiles/ summaries)
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get(args.workload, {}).get(top)
-        except Exception:
-            traffic = None
     # kernels per iteration of the batched step: preprocess, visible scan and compaction
     # (inside the cooperative sort when it runs), then either one cooperative launch
     # (visible-slot capacity within 8192 keys per SM and at most 256 super-tiles) that
@@ -640,7 +790,8 @@ def main():
     if not args.no_secondary:
         del bt
         torch.cuda.empty_cache()
-        line["secondary"] = [run_hypotheses(dev, flush), run_sequences(dev, flush)]
+        line["secondary"] = [run_hypotheses(dev, flush), run_sequences(dev, flush),
+                             run_sequence_tracking(dev, frames=args.sequence_frames)]
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(prob)
     if rank == 0:

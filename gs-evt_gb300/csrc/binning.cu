@@ -187,6 +187,7 @@ template <bool COARSE>
 __global__ void __launch_bounds__(GS_BLOCK) k_sorted_sums(BinParams p, const uint32_t *sorted_vals)
 {
     __shared__ uint32_t wsum[GS_BLOCK / 32], wsum2[GS_BLOCK / 32];
+    if (gs_sort_timed_out(p.ws.status)) return;  // the depth order is incomplete (uniform)
     const uint32_t nvis = p.ws.status[5];
     const uint32_t i = blockIdx.x * GS_BLOCK + threadIdx.x;
     uint32_t cnt = 0, scnt = 0;
@@ -251,6 +252,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sorted_sums(BinParams p, const uin
 __global__ void __launch_bounds__(GS_BLOCK) k_duplicate(BinParams p, const uint32_t *sorted_vals)
 {
     __shared__ uint32_t wtot[GS_BLOCK / 32];
+    if (gs_sort_timed_out(p.ws.status)) return;  // the depth order is incomplete (uniform)
     const uint32_t nvis = p.ws.status[5];
     const uint32_t i = blockIdx.x * GS_BLOCK + threadIdx.x;
     if (blockIdx.x * GS_BLOCK >= nvis) return;  // uniform per block
@@ -311,6 +313,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_duplicate(BinParams p, const uint3
 __global__ void __launch_bounds__(GS_BLOCK) k_duplicate_coarse(BinParams p, const uint32_t *sorted_vals)
 {
     __shared__ uint32_t wtot[GS_BLOCK / 32];
+    if (gs_sort_timed_out(p.ws.status)) return;  // the depth order is incomplete (uniform)
     const uint32_t nvis = p.ws.status[5];
     const uint32_t i = blockIdx.x * GS_BLOCK + threadIdx.x;
     if (blockIdx.x * GS_BLOCK >= nvis) return;  // uniform per block
@@ -421,6 +424,7 @@ __global__ void __launch_bounds__(FILTER_WARPS * 32) k_filter_tiles(const gsevt_
     __shared__ uint32_t s_cnt[FILTER_WARPS][FILTER_TILES + 1];  // [warp][tile]
     __shared__ uint32_t s_start[FILTER_TILES];
     const uint32_t sid = blockIdx.x;
+    if (gs_sort_timed_out(ws.status)) return;  // the super-tile lists are incomplete (uniform)
     if (sid >= ws.soffs[num_views]) return;  // uniform per block
     int lo = 0, hi = num_views - 1;
     while (lo < hi) {
@@ -509,8 +513,10 @@ __global__ void __launch_bounds__(FILTER_WARPS * 32) k_filter_tiles(const gsevt_
     }
 }
 
-__global__ void k_ranges(const uint32_t *keys, const uint32_t *count_word, uint32_t capacity, uint2 *ranges)
+__global__ void k_ranges(const uint32_t *keys, const uint32_t *count_word, uint32_t capacity, uint2 *ranges,
+                         const uint32_t *status)
 {
+    if (gs_sort_timed_out(status)) return;  // the keys' order is incomplete
     uint32_t K = min(*count_word, capacity);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
         uint32_t t = keys[i];
@@ -622,7 +628,7 @@ int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, 
     if (st) return st;
     if (buf != gs_tile_sort_buffer(L)) return GSEVT_ERR_ARG;
     int blocks = (int)std::min<uint32_t>((max_keys + 255) / 256, 152u * 16u);
-    k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status + 1, L.key_capacity, ws.ranges);
+    k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status + 1, L.key_capacity, ws.ranges, ws.status);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }
@@ -667,7 +673,7 @@ int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max
     if (st) return st;
     if (!one_pass) {
         int blocks = (int)std::min<uint32_t>((max_keys + 255) / 256, 152u * 16u);
-        k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status + 6, L.key_capacity, ws.sranges);
+        k_ranges<<<blocks, 256, 0, s>>>(ws.keys[buf], ws.status + 6, L.key_capacity, ws.sranges, ws.status);
     }
     k_filter_tiles<<<nsup, FILTER_WARPS * 32, 0, s>>>(f->views, L.num_views, ws, ws.vals[buf], ws.vals[buf ^ 1],
                                                      L.key_capacity);

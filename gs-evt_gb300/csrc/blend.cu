@@ -208,6 +208,7 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
     __shared__ Batch<RGB> sb[2];
     __shared__ gsevt_view V;
     const int tile = blockIdx.x;
+    if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
     if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
     __syncthreads();
     const int lt = tile - V.tile_offset;
@@ -401,6 +402,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
     __shared__ float acc[GS_BLOCK][NC + 1];
     __shared__ gsevt_view V;
     const int tile = blockIdx.x;
+    if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
     if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
     for (int i = threadIdx.x; i < GS_BLOCK * (NC + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
     __syncthreads();
@@ -439,7 +441,10 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
             const int other = V.pair_role == 0 ? pr.next_view : pr.last_view;
             const float Io = p.image[p.views[other].pix_offset + lp];
             const float Is = p.image[pix];
-            const float dI = V.pair_role == 0 ? (Io - Is) : (Is - Io);
+            // log grey: dI of the logs, and dI/dI_self carries 1 / (I_self + eps)
+            const bool lg = pr.log_grey != 0;
+            const float ls = lg ? logf(Is + pr.log_eps) : Is, lo = lg ? logf(Io + pr.log_eps) : Io;
+            const float dI = V.pair_role == 0 ? (lo - ls) : (ls - lo);
             const float e = (pr.unsigned_mode && pr.event_abs) ? pr.event_abs[lp] : pr.event[lp];
             const float n = dI * inv_s;
             float g;
@@ -449,7 +454,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
             } else {
                 g = (n - e) * inv_L;
             }
-            const float dd = (g - n * ng) * inv_s;
+            float dd = (g - n * ng) * inv_s;
+            if (lg) dd = __fdividef(dd, Is + pr.log_eps);
             gC[0] = V.pair_role == 0 ? -dd : dd;
         }
     }

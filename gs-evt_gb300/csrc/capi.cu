@@ -53,6 +53,7 @@ extern "C" size_t gsevt_workspace_bytes(const gsevt_layout *L)
 
 extern "C" int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -61,9 +62,11 @@ extern "C" int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream)
     cudaMemsetAsync(ws.status, 0, 64, s);
     cudaMemsetAsync(ws.sort_lookback, 0, (size_t)gs_lookback_tiles(f->L) * 256 * 8, s);
     if (f->L.num_pairs > 0) cudaMemsetAsync(ws.loss_done, 0, (size_t)f->L.num_pairs * 4, s);
-    // tile ranges always point inside the value buffers, even for a tile that a step
-    // whose layout check failed (GSEVT_STATUS_LAYOUT) leaves unwritten
+    // tile and super-tile ranges always point inside the value buffers, even where a step
+    // whose layout check failed (GSEVT_STATUS_LAYOUT) or whose sort gave up
+    // (GSEVT_STATUS_SORT_TIMEOUT) leaves them unwritten
     cudaMemsetAsync(ws.ranges, 0, (size_t)f->L.total_tiles * sizeof(uint2), s);
+    cudaMemsetAsync(ws.sranges, 0, (size_t)gs_super_bound(f->L) * sizeof(uint2), s);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }
@@ -98,6 +101,7 @@ extern "C" void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out)
 
 extern "C" int gsevt_clear_status(const gsevt_frame *f, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -108,6 +112,7 @@ extern "C" int gsevt_clear_status(const gsevt_frame *f, gsevt_stream_t stream)
 
 extern "C" int gsevt_read_status(const gsevt_frame *f, uint32_t *out2, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -120,6 +125,7 @@ extern "C" int gsevt_read_status(const gsevt_frame *f, uint32_t *out2, gsevt_str
 
 extern "C" int gsevt_preprocess_fwd(const gsevt_frame *f, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -133,6 +139,7 @@ extern "C" int gsevt_preprocess_fwd(const gsevt_frame *f, gsevt_stream_t stream)
 
 extern "C" int gsevt_bin_and_sort(const gsevt_frame *f, uint32_t max_keys, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -143,6 +150,7 @@ extern "C" int gsevt_bin_and_sort(const gsevt_frame *f, uint32_t max_keys, gsevt
 
 extern "C" int gsevt_blend_fwd(const gsevt_frame *f, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -151,6 +159,7 @@ extern "C" int gsevt_blend_fwd(const gsevt_frame *f, gsevt_stream_t stream)
 
 extern "C" int gsevt_loss_fwd(const gsevt_frame *f, double *loss_out, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -161,6 +170,7 @@ extern "C" int gsevt_loss_fwd(const gsevt_frame *f, double *loss_out, gsevt_stre
 extern "C" int gsevt_blend_bwd(const gsevt_frame *f, const float *dL_dimage, const float *dL_ddepth,
                                const float *dL_dalpha, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -174,6 +184,7 @@ extern "C" int gsevt_blend_bwd(const gsevt_frame *f, const float *dL_dimage, con
 extern "C" int gsevt_preprocess_bwd(const gsevt_frame *f, double *xi_out, const gsevt_map_grads *grads,
                                     gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;
@@ -191,6 +202,7 @@ extern "C" int gsevt_preprocess_bwd(const gsevt_frame *f, double *xi_out, const 
 extern "C" int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *poses, int32_t num_poses,
                                         double *loss_out, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     Workspace ws;
     int st = check_frame(f, &ws);
     if (st) return st;

@@ -116,6 +116,7 @@ struct Workspace {
     float4 *fcache;       // [num_vg][6] forward intermediates of each visible slot for the
                           // twist-only adjoint (frames with render pairs; else absent)
     size_t bytes;
+    uint32_t spin_limit;  // polls of a bounded wait before it gives up (the layout's, or GS_SPIN_LIMIT)
 };
 
 #define GS_WS_REGIONS 34
@@ -206,10 +207,20 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     w.sranges = (uint2 *)take((size_t)gs_super_bound(L) * 8);
     w.fcache = (L.num_pairs > 0 && !rgb) ? (float4 *)take(vg * GS_FCACHE * 16) : nullptr;
     w.bytes = off;
+    w.spin_limit = L.spin_limit ? L.spin_limit : GS_SPIN_LIMIT;
     return w;
 }
 
 // ------------------------------------------------------------- helpers ----------
+// True once a bounded wait of this frame's sorts ran out (GSEVT_STATUS_SORT_TIMEOUT).
+// The kernels that consume a sort's order then do nothing, so an index that a sort left
+// unwritten is never followed.  The word only changes inside the sort kernels, which
+// precede every reader on the stream, so all threads of a block read the same value.
+__device__ __forceinline__ bool gs_sort_timed_out(const uint32_t *status)
+{
+    return (__ldcg(status) & GSEVT_STATUS_SORT_TIMEOUT) != 0u;
+}
+
 __device__ __forceinline__ int gs_find_map(const gsevt_map *maps, int num_maps, int block)
 {
     int m = 0;
@@ -286,6 +297,12 @@ __device__ __forceinline__ double warp_sum_d(double v)
         cudaError_t _e = cudaGetLastError();                    \
         if (_e != cudaSuccess) return GSEVT_ERR_CUDA;           \
     } while (0)
+
+// First statement of every entry point that enqueues work: clears an error that an
+// earlier, unrelated runtime call of the caller left pending, so that GS_CUDA_CHECK
+// reports only failures of this call's own launches and copies.  (A sticky error, which
+// means the context is lost, is still reported by the next check.)
+#define GS_ENTRY() ((void)cudaGetLastError())
 
 // Prepares the cooperative sort on the current device (sort.cu); outside stream capture.
 void gs_sort_prepare();

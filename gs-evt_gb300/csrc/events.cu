@@ -16,6 +16,8 @@
 //      sampled bilinearly with a zero border.
 #include "common.cuh"
 
+#include <cuda.h>
+
 #include <mutex>
 
 #define EV_MAX_K 31
@@ -164,6 +166,62 @@ inline int ev_norm_blocks(int W, int H)
     return (int)std::min<size_t>((P + 255) / 256, 152 * 8);
 }
 
+// Argument checks shared by both entry points; nothing is enqueued before they pass.
+int ev_check(int64_t n, const uint16_t *x, const uint16_t *y, const uint8_t *polarity, int32_t width, int32_t height,
+             const double *camera, int32_t ksize, int32_t levels, const float *out_signed)
+{
+    if (width <= 0 || height <= 0 || ksize < 1 || (ksize & 1) == 0 || ksize > EV_MAX_K || levels < 1 ||
+        !out_signed || n < 0 || (n > 0 && (!x || !y || !polarity)))
+        return GSEVT_ERR_ARG;
+    for (int l = 1; l < levels; ++l)
+        if ((int)(width * (1.0 / (1 << l))) < 1 || (int)(height * (1.0 / (1 << l))) < 1) return GSEVT_ERR_ARG;
+    if (camera && !(camera[0] != 0.0 && camera[1] != 0.0)) return GSEVT_ERR_ARG;
+    return GSEVT_OK;
+}
+
+// The launch sequence of the event frame over a scratch area at `base` (carved by
+// ev_carve), for arguments that passed ev_check: clear the count image, count, undistort
+// or convert, blur, normalise and write the pyramid.
+int ev_enqueue(void *base, int64_t n, const uint16_t *x, const uint16_t *y, const uint8_t *polarity, int32_t width,
+               int32_t height, const double *camera, int32_t ksize, int32_t levels, float *out_signed,
+               float *out_unsigned, cudaStream_t s)
+{
+    EvScratch sc = ev_carve(base, width, height);
+    Kern k;
+    k.r = ksize / 2;
+    double sigma = 0.3 * ((ksize - 1) * 0.5 - 1.0) + 0.8, ws[EV_MAX_K], sum = 0.0;
+    for (int i = 0; i < ksize; ++i) {
+        double xx = i - k.r;
+        ws[i] = exp(-(xx * xx) / (2.0 * sigma * sigma));
+        sum += ws[i];
+    }
+    for (int i = 0; i < EV_MAX_K; ++i) k.w[i] = i < ksize ? (float)(ws[i] / sum) : 0.0f;
+    const size_t P = (size_t)width * height;
+    // the count image accumulates with atomics and must start at zero on every call
+    if (cudaMemsetAsync(sc.count, 0, P * 4, s) != cudaSuccess) return GSEVT_ERR_CUDA;
+    if (n > 0) {
+        int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)152 * 8);
+        k_ev_count<<<blocks, 256, 0, s>>>(n, x, y, polarity, width, height, sc.count);
+        GS_CUDA_CHECK();
+    }
+    dim3 gh((width + 127) / 128, height);
+    if (camera) {
+        Cam c = {camera[0], camera[1], camera[2], camera[3], camera[4], camera[5], camera[6], camera[7], camera[8]};
+        k_ev_undistort<<<gh, 128, 0, s>>>(sc.count, width, height, c, sc.img);
+    } else {
+        k_ev_to_float<<<(int)std::min<size_t>((P + 255) / 256, 152 * 8), 256, 0, s>>>(sc.count, P, sc.img);
+    }
+    GS_CUDA_CHECK();
+    k_ev_blur_h<<<gh, 128, 0, s>>>(sc.img, width, height, k, sc.tmp);
+    GS_CUDA_CHECK();
+    k_ev_blur_v<<<EV_PART_BLOCKS, 256, 0, s>>>(sc.tmp, width, height, k, sc.blur, sc.part);
+    GS_CUDA_CHECK();
+    k_ev_normalize<<<ev_norm_blocks(width, height), 256, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height,
+                                                                 levels, out_signed, out_unsigned);
+    GS_CUDA_CHECK();
+    return GSEVT_OK;
+}
+
 }  // namespace
 
 extern "C" size_t gsevt_event_scratch_bytes(int32_t width, int32_t height)
@@ -177,123 +235,105 @@ extern "C" int gsevt_events_accumulate(int64_t n, const uint16_t *x, const uint1
                                        int32_t levels, void *scratch, float *out_signed, float *out_unsigned,
                                        gsevt_stream_t stream)
 {
-    cudaStream_t s = (cudaStream_t)stream;
-    if (width <= 0 || height <= 0 || ksize < 1 || (ksize & 1) == 0 || ksize > EV_MAX_K || levels < 1 ||
-        !scratch || !out_signed || n < 0 || (n > 0 && (!x || !y || !polarity)))
-        return GSEVT_ERR_ARG;
-    for (int l = 1; l < levels; ++l)
-        if ((int)(width * (1.0 / (1 << l))) < 1 || (int)(height * (1.0 / (1 << l))) < 1) return GSEVT_ERR_ARG;
-    EvScratch sc = ev_carve(scratch, width, height);
-    Kern k;
-    k.r = ksize / 2;
-    double sigma = 0.3 * ((ksize - 1) * 0.5 - 1.0) + 0.8, ws[EV_MAX_K], sum = 0.0;
-    for (int i = 0; i < ksize; ++i) {
-        double xx = i - k.r;
-        ws[i] = exp(-(xx * xx) / (2.0 * sigma * sigma));
-        sum += ws[i];
-    }
-    for (int i = 0; i < EV_MAX_K; ++i) k.w[i] = i < ksize ? (float)(ws[i] / sum) : 0.0f;
-    size_t P = (size_t)width * height;
-    cudaMemsetAsync(sc.count, 0, P * 4, s);
-    GS_CUDA_CHECK();
-    if (n > 0) {
-        int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)152 * 8);
-        k_ev_count<<<blocks, 256, 0, s>>>(n, x, y, polarity, width, height, sc.count);
-        GS_CUDA_CHECK();
-    }
-    dim3 gh((width + 127) / 128, height);
-    if (camera) {
-        Cam c = {camera[0], camera[1], camera[2], camera[3], camera[4], camera[5], camera[6], camera[7], camera[8]};
-        if (!(c.fx != 0.0 && c.fy != 0.0)) return GSEVT_ERR_ARG;
-        k_ev_undistort<<<gh, 128, 0, s>>>(sc.count, width, height, c, sc.img);
-    } else {
-        k_ev_to_float<<<(int)std::min<size_t>((P + 255) / 256, 152 * 8), 256, 0, s>>>(sc.count, P, sc.img);
-    }
-    k_ev_blur_h<<<gh, 128, 0, s>>>(sc.img, width, height, k, sc.tmp);
-    k_ev_blur_v<<<EV_PART_BLOCKS, 256, 0, s>>>(sc.tmp, width, height, k, sc.blur, sc.part);
-    k_ev_normalize<<<ev_norm_blocks(width, height), 256, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height,
-                                                                 levels, out_signed, out_unsigned);
-    GS_CUDA_CHECK();
-    return GSEVT_OK;
+    GS_ENTRY();
+    int rc = ev_check(n, x, y, polarity, width, height, camera, ksize, levels, out_signed);
+    if (rc != GSEVT_OK) return rc;
+    if (!scratch) return GSEVT_ERR_ARG;
+    return ev_enqueue(scratch, n, x, y, polarity, width, height, camera, ksize, levels, out_signed, out_unsigned,
+                      (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------------------------
-// gsevt_events_accumulate_noalloc: the same launches with scratch in a fixed
-// library-owned device buffer instead of caller memory, for callers that cannot
-// allocate (see the declaration in gsevt.h).  The buffer is one per device (a
-// __device__ variable exists once per context the module is loaded into); its address
-// is looked up once per device and cached.  Concurrent calls on one device race on it.
+// gsevt_events_accumulate_noalloc: the launch sequence above over a fixed library-owned
+// device buffer instead of caller scratch, for callers that cannot allocate (see the
+// declaration in gsevt.h).  A __device__ variable exists once in every CUDA context the
+// module is loaded into, so its address is a property of the context: it is resolved
+// with cudaGetSymbolAddress the first time a call runs in a context and cached under that
+// context's unique id (cuCtxGetId; ids are never reused within a process, so a context
+// created after cudaDeviceReset, or one a driver-API caller made current, resolves its
+// own address).  Calls that overlap on the GPU share the buffer and race.
 
-#define EV_NOALLOC_MAX_DEVICES 64
+#define EV_NOALLOC_CONTEXTS 64
 #define EV_NOALLOC_BYTES (4 * ((((size_t)GSEVT_EVENTS_NOALLOC_MAX_PIXELS * 4) + 255) & ~(size_t)255) + \
                           (((size_t)EV_PART_BLOCKS * 8 + 255) & ~(size_t)255))
 
 static __device__ __align__(256) unsigned char g_ev_noalloc_scratch[EV_NOALLOC_BYTES];
-static void *g_ev_noalloc_addr[EV_NOALLOC_MAX_DEVICES];
-static std::mutex g_ev_noalloc_mu;
 
-static int ev_noalloc_scratch(void **out)
+namespace {
+
+// driver entry points, resolved through the runtime (the library links only cudart)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *ctx);
+typedef CUresult (*CtxGetIdFn)(CUcontext ctx, unsigned long long *id);
+
+struct NoallocCache {
+    std::mutex mu;
+    CtxGetCurrentFn get_current = nullptr;
+    CtxGetIdFn get_id = nullptr;
+    bool resolved = false;
+    int used = 0, next = 0;
+    unsigned long long ids[EV_NOALLOC_CONTEXTS];
+    void *addr[EV_NOALLOC_CONTEXTS];
+};
+NoallocCache g_noalloc;
+
+// Address of the fixed buffer in the calling thread's current context (the current
+// device's primary context when none is current yet).
+int ev_noalloc_scratch(void **out)
 {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess) return GSEVT_ERR_CUDA;
-    if (dev < 0 || dev >= EV_NOALLOC_MAX_DEVICES) return GSEVT_ERR_ARG;
-    std::lock_guard<std::mutex> lock(g_ev_noalloc_mu);
-    if (!g_ev_noalloc_addr[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_ev_noalloc_scratch) != cudaSuccess || !p) return GSEVT_ERR_CUDA;
-        g_ev_noalloc_addr[dev] = p;
+    std::lock_guard<std::mutex> lock(g_noalloc.mu);
+    if (!g_noalloc.resolved) {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+            qb != cudaDriverEntryPointSuccess || !a || !b)
+            return GSEVT_ERR_CUDA;
+        g_noalloc.get_current = (CtxGetCurrentFn)a;
+        g_noalloc.get_id = (CtxGetIdFn)b;
+        g_noalloc.resolved = true;
     }
-    *out = g_ev_noalloc_addr[dev];
+    CUcontext ctx = nullptr;
+    if (g_noalloc.get_current(&ctx) != CUDA_SUCCESS) return GSEVT_ERR_CUDA;
+    if (!ctx) {
+        // no context on this thread yet: bind the current device's primary context
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) return GSEVT_ERR_CUDA;
+        if (g_noalloc.get_current(&ctx) != CUDA_SUCCESS || !ctx) return GSEVT_ERR_CUDA;
+    }
+    unsigned long long id = 0;
+    if (g_noalloc.get_id(ctx, &id) != CUDA_SUCCESS) return GSEVT_ERR_CUDA;
+    for (int i = 0; i < g_noalloc.used; ++i)
+        if (g_noalloc.ids[i] == id) {
+            *out = g_noalloc.addr[i];
+            return GSEVT_OK;
+        }
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_ev_noalloc_scratch) != cudaSuccess || !p) return GSEVT_ERR_CUDA;
+    // a full table overwrites its entries in turn, oldest first
+    const int slot = g_noalloc.next;
+    g_noalloc.next = (g_noalloc.next + 1) % EV_NOALLOC_CONTEXTS;
+    if (g_noalloc.used < EV_NOALLOC_CONTEXTS) ++g_noalloc.used;
+    g_noalloc.ids[slot] = id;
+    g_noalloc.addr[slot] = p;
+    *out = p;
     return GSEVT_OK;
 }
+
+}  // namespace
 
 extern "C" int gsevt_events_accumulate_noalloc(int64_t n, const uint16_t *x, const uint16_t *y,
                                                const uint8_t *polarity, int32_t width, int32_t height,
                                                const double *camera, int32_t ksize, int32_t levels,
                                                float *out_signed, float *out_unsigned, gsevt_stream_t stream)
 {
-    cudaStream_t s = (cudaStream_t)stream;
-    if (width <= 0 || height <= 0 || ksize < 1 || (ksize & 1) == 0 || ksize > EV_MAX_K || levels < 1 ||
-        !out_signed || n < 0 || (n > 0 && (!x || !y || !polarity)))
-        return GSEVT_ERR_ARG;
-    if ((int64_t)width * height > (int64_t)GSEVT_EVENTS_NOALLOC_MAX_PIXELS) return GSEVT_ERR_TOO_LARGE;
-    for (int l = 1; l < levels; ++l)
-        if ((int)(width * (1.0 / (1 << l))) < 1 || (int)(height * (1.0 / (1 << l))) < 1) return GSEVT_ERR_ARG;
-    Cam c = {};
-    if (camera) {
-        c = {camera[0], camera[1], camera[2], camera[3], camera[4], camera[5], camera[6], camera[7], camera[8]};
-        if (!(c.fx != 0.0 && c.fy != 0.0)) return GSEVT_ERR_ARG;
-    }
-    void *base = nullptr;
-    int rc = ev_noalloc_scratch(&base);
+    int rc = ev_check(n, x, y, polarity, width, height, camera, ksize, levels, out_signed);
     if (rc != GSEVT_OK) return rc;
-    EvScratch sc = ev_carve(base, width, height);
-    Kern k;
-    k.r = ksize / 2;
-    double sigma = 0.3 * ((ksize - 1) * 0.5 - 1.0) + 0.8, ws[EV_MAX_K], sum = 0.0;
-    for (int i = 0; i < ksize; ++i) {
-        double xx = i - k.r;
-        ws[i] = exp(-(xx * xx) / (2.0 * sigma * sigma));
-        sum += ws[i];
-    }
-    for (int i = 0; i < EV_MAX_K; ++i) k.w[i] = i < ksize ? (float)(ws[i] / sum) : 0.0f;
-    size_t P = (size_t)width * height;
-    // the count image accumulates with atomics and must start at zero on every call
-    if (cudaMemsetAsync(sc.count, 0, P * 4, s) != cudaSuccess) return GSEVT_ERR_CUDA;
-    if (n > 0) {
-        int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)152 * 8);
-        k_ev_count<<<blocks, 256, 0, s>>>(n, x, y, polarity, width, height, sc.count);
-        GS_CUDA_CHECK();
-    }
-    dim3 gh((width + 127) / 128, height);
-    if (camera)
-        k_ev_undistort<<<gh, 128, 0, s>>>(sc.count, width, height, c, sc.img);
-    else
-        k_ev_to_float<<<(int)std::min<size_t>((P + 255) / 256, 152 * 8), 256, 0, s>>>(sc.count, P, sc.img);
-    k_ev_blur_h<<<gh, 128, 0, s>>>(sc.img, width, height, k, sc.tmp);
-    k_ev_blur_v<<<EV_PART_BLOCKS, 256, 0, s>>>(sc.tmp, width, height, k, sc.blur, sc.part);
-    k_ev_normalize<<<ev_norm_blocks(width, height), 256, 0, s>>>(sc.blur, sc.part, EV_PART_BLOCKS, width, height,
-                                                                 levels, out_signed, out_unsigned);
-    GS_CUDA_CHECK();
-    return GSEVT_OK;
+    if ((int64_t)width * height > (int64_t)GSEVT_EVENTS_NOALLOC_MAX_PIXELS) return GSEVT_ERR_TOO_LARGE;
+    GS_ENTRY();
+    void *base = nullptr;
+    rc = ev_noalloc_scratch(&base);
+    if (rc != GSEVT_OK) return rc;
+    return ev_enqueue(base, n, x, y, polarity, width, height, camera, ksize, levels, out_signed, out_unsigned,
+                      (cudaStream_t)stream);
 }

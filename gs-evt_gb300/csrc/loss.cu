@@ -1,6 +1,7 @@
 // Normalised intensity-change loss of every render pair, in one launch.
 //
 // Replaces utils/render_camera/frame.py:86-94 (dI = I_next - I_last, n = dI/||dI||,
+// or with the pair's log_grey the log-intensity change ln(I_next + eps) - ln(I_last + eps),
 // |n|) and utils/tracker.py:93-103 (L = ||n - E|| or || |n| - |E| ||), which run as
 // ~8 forward and ~10 backward torch kernels per iteration.  With s = ||dI||,
 // c = sum(dI E) (signed) or sum(|dI| |E|) (unsigned) and e2 = sum(E^2),
@@ -8,6 +9,7 @@
 // so one reduction pass gives L (FP32 over each thread's 8 pixels, float pairs with
 // error-free additions within a block, FP64 across blocks); the per-pixel gradient
 //   dL/dI_next = -dL/dI_last = (g - n (n.g)) / s,  n.g = (1 - c/s) / L,
+// (times 1 / (I + eps) of the view's own pixel in log mode)
 // is formed inside the blend adjoint without another pass, from 1/s, n.g and 1/L that
 // the last block rounds to FP32 once per pair (no FP64 arithmetic per pixel).
 // Each block reduces a slice of one pair into FP64 partials; the last block of the
@@ -35,6 +37,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     __shared__ FP2 part[GS_BLOCK / 32][3];
     __shared__ double dpart[GS_BLOCK / 32][3];
     __shared__ bool is_last;
+    if (gs_sort_timed_out(ws.status)) return;  // no images were rendered (uniform)
     const int b = blockIdx.x;
     const int pi = find_pair(pairs, num_pairs, b);
     const gsevt_pair pr = pairs[pi];
@@ -46,10 +49,13 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     float s2 = 0.0f, cr = 0.0f, e2 = 0.0f;
     const int base = lb * GS_BLOCK * LOSS_PIX_PER_THREAD;
 #pragma unroll
+    const bool lg = pr.log_grey != 0;
+    const float eps = pr.log_eps;
     for (int k = 0; k < LOSS_PIX_PER_THREAD; ++k) {
         int i = base + k * GS_BLOCK + threadIdx.x;
         if (i < P) {
-            float d = image[Vn.pix_offset + i] - image[Vl.pix_offset + i];
+            const float In = image[Vn.pix_offset + i], Il = image[Vl.pix_offset + i];
+            float d = lg ? logf(In + eps) - logf(Il + eps) : In - Il;
             float e = (pr.unsigned_mode && pr.event_abs) ? __ldg(pr.event_abs + i) : __ldg(pr.event + i);
             s2 = fmaf(d, d, s2);
             e2 = fmaf(e, e, e2);

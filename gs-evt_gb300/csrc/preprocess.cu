@@ -474,6 +474,7 @@ __global__ void __launch_bounds__(GS_BLOCK, MAPGRAD ? 1 : 2) k_preprocess_bwd(Bw
     __shared__ gsevt_view V;
     __shared__ float wpart[GS_BLOCK / 32][6];
     int b = blockIdx.x;
+    if (gs_sort_timed_out(p.ws.status)) return;  // no blend adjoint ran (uniform)
     if (threadIdx.x == 0) M = p.maps[gs_find_map(p.maps, p.num_maps, b)];
     __syncthreads();
     int m = gs_find_map(p.maps, p.num_maps, b);
@@ -756,6 +757,7 @@ extern "C" int gsevt_pack_map(int32_t n, const float *xyz, const float *opacity,
                               const float *rotations, const float *cov3d, const float *shs,
                               int32_t sh_coeffs, float scale_modifier, void *packed, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     if (n < 0 || !xyz || !opacity || !shs || !packed || sh_coeffs <= 0) return GSEVT_ERR_ARG;
     if (!cov3d && (!scales || !rotations)) return GSEVT_ERR_ARG;
     if (((uintptr_t)packed & 15) != 0) return GSEVT_ERR_ARG;

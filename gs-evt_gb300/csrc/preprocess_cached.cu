@@ -24,6 +24,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_preprocess_bwd_cached(CachedParams
     __shared__ int s_n;
     __shared__ float wpart[GS_BLOCK / 32][6];
     const int b = blockIdx.x;
+    if (gs_sort_timed_out(p.ws.status)) return;  // no blend adjoint ran (uniform)
     if (threadIdx.x == 0) {
         int lo = 0, hi = p.num_views - 1;
         while (lo < hi) {

@@ -19,8 +19,10 @@
 // Look-back entries are single 64-bit words {epoch:32 | flag:2 | count:30}; the epoch
 // changes every pass, so the table never needs clearing between passes or sorts (it
 // must be zero-filled once, when the workspace is created).  Every wait on a
-// predecessor is bounded by GS_SPIN_LIMIT polls; on expiry the block records
-// GSEVT_STATUS_SORT_TIMEOUT and continues, so a fault can never hang the GPU.
+// predecessor is bounded by the layout's spin limit (GS_SPIN_LIMIT polls by default); on
+// expiry the block records GSEVT_STATUS_SORT_TIMEOUT and continues with a partial prefix,
+// which only moves its scatter positions down (they stay inside [0, K)), so a fault can
+// never hang the GPU; the kernels that consume the order skip their work afterwards.
 // Stability: ranks follow (warp, key slot, lane) order, which is the input order.
 #include <atomic>
 
@@ -67,6 +69,7 @@ struct PassParams {
     int pass;
     uint2 *ranges;              // single-pass sorts: [start, end) of keys 0..nranges-1, or null
     uint32_t nranges;
+    uint32_t spin_limit;        // polls of the look-back wait before it gives up
 };
 
 template <typename KT, int SORT_KPT>
@@ -184,7 +187,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
             unsigned long long e = lb[(size_t)t * 256 + d];
             unsigned long long fl = (e >> 30) & 3ull;
             if ((e >> 32) != epoch || fl == 0) {
-                if (++spins > GS_SPIN_LIMIT) {
+                if (++spins > p.spin_limit) {
                     atomicOr(p.status, GSEVT_STATUS_SORT_TIMEOUT);
                     break;
                 }
@@ -255,8 +258,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_sort_pass(PassParams<KT> p)
 // There is no histogram kernel, no per-pass launch and no look-back chain, and no block
 // reads more of the table than its own column and the rows it scans.  A pass whose digit
 // is constant is the identity permutation here as well.  Barriers are an arrival counter
-// (release add, acquire loads); every wait is bounded by GS_SPIN_LIMIT polls, after which
-// the block records GSEVT_STATUS_SORT_TIMEOUT and continues.  Data written by other blocks
+// (release add, acquire loads); every wait is bounded by the layout's spin limit, after
+// which the block records GSEVT_STATUS_SORT_TIMEOUT and returns at once.  A block that
+// passes a barrier has seen every block arrive there, so no block had given up earlier
+// and the data it reads is complete; the blocks still running then give up at the next
+// barrier, which the returned block never reaches.  Every scatter is also bounded by the
+// capacity.  Data written by other blocks
 // in an earlier phase is read with ld.global.cg (L2), never through a stale L1 line.
 // Optional tail of the depth sort in the batched tracker (gs_launch_depth_order with
 // coarse binning): after the last pass the same grid bins the depth-sorted slots through
@@ -280,6 +287,7 @@ struct CoopParams {
     uint32_t *status;
     const uint32_t *count;  // number of keys (device word)
     uint32_t capacity;
+    uint32_t spin_limit;    // polls of a barrier wait before it gives up
     int passes;
     CoopBin bin;
     GsCompact cmp;
@@ -291,20 +299,27 @@ __device__ __forceinline__ void coop_arrive(uint32_t *ctr)
     if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
 }
 
-__device__ __forceinline__ void coop_wait(const uint32_t *ctr, uint32_t target, uint32_t *status)
+// Waits (thread 0, bounded) until `target` arrivals; returns false, uniformly over the
+// block, when the wait ran out (the status bit is then set and the block must return).
+__device__ __forceinline__ bool coop_wait(const uint32_t *ctr, uint32_t target, uint32_t *status, uint32_t limit)
 {
+    __shared__ int s_go;
     if (threadIdx.x == 0) {
         uint32_t spins = 0, v;
+        int go = 1;
         for (;;) {
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
             if (v >= target) break;
-            if (++spins > GS_SPIN_LIMIT) {
+            if (++spins > limit) {
                 atomicOr(status, GSEVT_STATUS_SORT_TIMEOUT);
+                go = 0;
                 break;
             }
         }
+        s_go = go;
     }
     __syncthreads();
+    return s_go != 0;
 }
 
 // exclusive scan of one value per thread over threads 0-255 (the digits); every thread
@@ -605,7 +620,7 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
                 svals[pos] = sin[(uint32_t)w * span + (uint32_t)(k * 32 + lane)];
             }
         }
-        coop_wait(p.barrier, nbar * G, p.status);
+        if (!coop_wait(p.barrier, nbar * G, p.status, p.spin_limit)) return;
         // rows b, b + G, ... of the table: exclusive prefix over the blocks, in place, and
         // the row total (warp i takes row b + i G; lane l holds columns l, l + 32, ...)
         {
@@ -636,7 +651,7 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
         }
         coop_arrive(p.barrier);
         ++nbar;
-        coop_wait(p.barrier, nbar * G, p.status);
+        if (!coop_wait(p.barrier, nbar * G, p.status, p.spin_limit)) return;
         uint32_t A = 0, E = 0;
         if (tid < 256) {
             E = __ldcg(p.cnt + (size_t)d * GS_COOP_GP + b);
@@ -652,12 +667,15 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
         for (uint32_t i = tid; i < nwrite; i += GS_COOP_THREADS) {
             const uint32_t kk = skeys[i];
             const uint32_t dg = (kk >> shift) & 255u;
-            kout[gbase[dg] + (i - dstart[dg])] = kk;
-            vout[gbase[dg] + (i - dstart[dg])] = svals[i];
+            const uint32_t pos = gbase[dg] + (i - dstart[dg]);
+            if (pos < p.capacity) {
+                kout[pos] = kk;
+                vout[pos] = svals[i];
+            }
         }
         if (compact) {
             // the visible slots are now keys [0, K) of buffer 1: the runs of the later passes
-            K = s_total[1];
+            K = min(s_total[1], p.capacity);
             if (b == 0 && tid == 0) p.status[5] = K;  // N_vis
             TS = (K + G - 1) / G;
             t0 = min(K, b * TS);
@@ -668,7 +686,7 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
         if (pass + 1 < p.passes) {
             coop_arrive(p.barrier);
             ++nbar;
-            coop_wait(p.barrier, nbar * G, p.status);
+            if (!coop_wait(p.barrier, nbar * G, p.status, p.spin_limit)) return;
         }
     }
     if (K == 0) {  // no visible slot (uniform; only reachable with the compaction in pass 0)
@@ -685,7 +703,7 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
     coop_arrive(p.barrier);
     ++nbar;
     for (int i = tid; i < COOP_WARPS * 256; i += GS_COOP_THREADS) (&whist[0][0])[i] = 0;
-    coop_wait(p.barrier, nbar * G, p.status);
+    if (!coop_wait(p.barrier, nbar * G, p.status, p.spin_limit)) return;
     const int nviews = min(p.bin.num_views, COOP_MAX_VIEWS);  // the launcher checks the count
     if (tid < nviews) {
         const gsevt_view &V = p.bin.views[tid];
@@ -755,7 +773,7 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
     if (q == 0) p.cnt[(size_t)d * GS_COOP_GP + b] = tot;
     coop_arrive(p.barrier);
     ++nbar;
-    coop_wait(p.barrier, nbar * G, p.status);
+    if (!coop_wait(p.barrier, nbar * G, p.status, p.spin_limit)) return;
     {
         const uint32_t r = b + (uint32_t)w * G;
         if (r < 256) {
@@ -784,7 +802,7 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
     }
     coop_arrive(p.barrier);
     ++nbar;
-    coop_wait(p.barrier, nbar * G, p.status);
+    if (!coop_wait(p.barrier, nbar * G, p.status, p.spin_limit)) return;
     uint32_t A = 0, E = 0;
     if (tid < 256) {
         E = __ldcg(p.cnt + (size_t)d * GS_COOP_GP + b);
@@ -879,6 +897,7 @@ bool launch_coop(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_
     cp.status = ws.status;
     cp.count = count;
     cp.capacity = capacity;
+    cp.spin_limit = ws.spin_limit;
     cp.passes = passes;
     cp.cmp = {};
     if (cmp) {
@@ -1004,6 +1023,7 @@ int gs_launch_sort_t(KT *const keys[2], uint32_t *const vals[2], const uint32_t 
         p.pass = pass;
         p.ranges = ranges;
         p.nranges = nranges;
+        p.spin_limit = ws.spin_limit;
         if (kpt == 4) k_sort_pass<KT, 4><<<tiles, GS_BLOCK, 0, s>>>(p);
         else if (kpt == 8) k_sort_pass<KT, 8><<<tiles, GS_BLOCK, 0, s>>>(p);
         else k_sort_pass<KT, 12><<<tiles, GS_BLOCK, 0, s>>>(p);

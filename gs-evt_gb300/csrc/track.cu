@@ -195,6 +195,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
     constexpr int WORDS = (int)(sizeof(gsevt_pose_state) / 4);
     const int pi = blockIdx.x;
     if (pi >= num_poses) return;
+    // the iteration's sort gave up: leave the pose state as it is (uniform)
+    if (gs_sort_timed_out(ws.status)) return;
     if (poses[pi].control && poses[pi].frozen) return;  // this problem's level is finished (uniform)
     for (int i = threadIdx.x; i < WORDS; i += GS_BLOCK)
         ((uint32_t *)&S)[i] = ((const uint32_t *)(poses + pi))[i];
@@ -490,6 +492,7 @@ int gs_launch_track_finalize(const gsevt_frame *f, const Workspace &ws, gsevt_po
 extern "C" int gsevt_track_init_views(gsevt_view *views, const gsevt_pose_state *poses, int32_t num_poses,
                                       gsevt_stream_t stream)
 {
+    GS_ENTRY();
     if (!views || !poses || num_poses <= 0) return GSEVT_ERR_ARG;
     k_track_views<<<(num_poses + 63) / 64, 64, 0, (cudaStream_t)stream>>>(views, poses, num_poses);
     GS_CUDA_CHECK();
@@ -500,6 +503,7 @@ extern "C" int gsevt_chain_view_grad(const double *xi, const float *vel_transfor
                                      const float *linear_vel, const float *angular_vel, float *out12,
                                      gsevt_stream_t stream)
 {
+    GS_ENTRY();
     if (!xi || !vel_transform_t || !linear_vel || !angular_vel || !out12) return GSEVT_ERR_ARG;
     k_chain_view<<<1, 1, 0, (cudaStream_t)stream>>>(xi, vel_transform_t, delta_time, linear_vel, angular_vel, out12);
     GS_CUDA_CHECK();
@@ -511,6 +515,7 @@ extern "C" int gsevt_view_from_settings(const float *viewmatrix_t, const float *
                                         int32_t tile_offset, int32_t pix_offset, int32_t map, int32_t vg_offset,
                                         int32_t sb_offset, gsevt_view *view_out, gsevt_stream_t stream)
 {
+    GS_ENTRY();
     if (!viewmatrix_t || !projmatrix_raw_t || !campos || !view_out || width <= 0 || height <= 0) return GSEVT_ERR_ARG;
     k_view_from_settings<<<1, 1, 0, (cudaStream_t)stream>>>(viewmatrix_t, projmatrix_raw_t, campos, bg, tanfovx, tanfovy,
                                                            width, height, tile_offset, pix_offset, map, vg_offset,

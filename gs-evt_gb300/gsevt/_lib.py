@@ -18,6 +18,7 @@ ERRORS = {
     -4: "bounded device wait ran out",
     -5: "CUDA launch or copy failed",
     -6: "workspace smaller than gsevt_workspace_bytes",
+    -7: "frame larger than the fixed scratch buffer holds",
 }
 STATUS_KEY_OVERFLOW = 1
 STATUS_SORT_TIMEOUT = 2
@@ -73,7 +74,8 @@ class MapGrads(C.Structure):
 class Pair(C.Structure):
     _fields_ = [("last_view", C.c_int32), ("next_view", C.c_int32), ("event", C.c_void_p),
                 ("event_abs", C.c_void_p), ("unsigned_mode", C.c_int32), ("pose", C.c_int32),
-                ("block_offset", C.c_int32), ("num_blocks", C.c_int32)]
+                ("block_offset", C.c_int32), ("num_blocks", C.c_int32), ("log_grey", C.c_int32),
+                ("log_eps", C.c_float)]
 
 
 class Layout(C.Structure):
@@ -81,7 +83,8 @@ class Layout(C.Structure):
                 ("num_vg", C.c_int32), ("num_scan_blocks", C.c_int32),
                 ("preprocess_blocks", C.c_int32), ("total_tiles", C.c_int32),
                 ("total_pixels", C.c_int32), ("channels", C.c_int32), ("sort_bits", C.c_int32),
-                ("key_capacity", C.c_uint32), ("loss_blocks", C.c_int32), ("super_tiles", C.c_int32)]
+                ("key_capacity", C.c_uint32), ("loss_blocks", C.c_int32), ("super_tiles", C.c_int32),
+                ("spin_limit", C.c_uint32)]
 
 
 class Frame(C.Structure):

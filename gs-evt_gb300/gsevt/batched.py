@@ -26,7 +26,7 @@ class Problem:
     """One tracking problem: map index, current pose / velocity, event frames, camera."""
 
     def __init__(self, map_index, R, t, lin_vel, ang_vel, delta_tau, width, height, fx, fy, event_signed,
-                 event_unsigned=None, lr=DEFAULT_LR, opt_vel=True, unsigned=False):
+                 event_unsigned=None, lr=DEFAULT_LR, opt_vel=True, unsigned=False, log_eps=None):
         self.map_index = map_index
         self.R, self.t = np.asarray(R, np.float64), np.asarray(t, np.float64)
         self.lin_vel, self.ang_vel = np.asarray(lin_vel, np.float64), np.asarray(ang_vel, np.float64)
@@ -35,6 +35,8 @@ class Problem:
         self.event_signed = event_signed.reshape(-1).contiguous().float()
         self.event_unsigned = None if event_unsigned is None else event_unsigned.reshape(-1).contiguous().float()
         self.lr, self.opt_vel, self.unsigned = lr, bool(opt_vel), bool(unsigned)
+        # None: the reference's linear grey change; eps > 0: ln(I_next + eps) - ln(I_last + eps)
+        self.log_eps = log_eps
 
 
 def _field(name):
@@ -72,7 +74,7 @@ class BatchedTracker:
                                       campos=np.zeros(3), tanfovx=np.tan(fovx / 2), tanfovy=np.tan(fovy / 2),
                                       pair=i, pair_role=role))
             pairs.append({"last": 2 * i, "next": 2 * i + 1, "event": p.event_signed, "event_abs": p.event_unsigned,
-                          "unsigned": p.unsigned, "pose": i})
+                          "unsigned": p.unsigned, "pose": i, "log_eps": p.log_eps})
         self.frame = GSFrame(specs, views, channels=1, pairs=pairs, key_capacity=key_capacity or (1 << 20),
                              device=self.device)
         self.num = len(self.problems)
@@ -177,12 +179,13 @@ class BatchedSequenceTracker:
     on the device for all problems in lockstep (finished problems are frozen), and after
     five frames the weighted velocity update (camera.py:157-181).
 
-    cameras: list of (map_index, width, height, fx, fy) per problem.  One frame per pyramid
+    cameras: list of (map_index, width, height, fx, fy) per problem.  log_eps selects the
+    log-intensity change (as Problem).  One frame per pyramid
     level shares the maps and one device pose-state array; each level's iteration is a
     CUDA graph captured once and replayed for every frame."""
 
     def __init__(self, maps, cameras, lr=DEFAULT_LR, max_optim_iter=200, converged_threshold=1e-4, levels=3,
-                 poll_every=10, device="cuda"):
+                 poll_every=10, device="cuda", log_eps=None):
         from .pose import exp_se3
         self.device = torch.device(device)
         self.levels, self.max_iter, self.thr, self.poll = levels, int(max_optim_iter), float(converged_threshold), poll_every
@@ -208,7 +211,7 @@ class BatchedSequenceTracker:
                 eu = torch.zeros(w * h, dtype=torch.float32, device=self.device)
                 bufs.append((es, eu))
                 probs.append(Problem(mi, np.eye(3), np.zeros(3), np.zeros(3), np.zeros(3), 0.01, w, h, fx * sc,
-                                     fy * sc, es, eu, lr=lr))
+                                     fy * sc, es, eu, lr=lr, log_eps=log_eps))
             self.ev.append(bufs)
             # capacity is fitted on the first frame
             self.trackers.append(BatchedTracker(self.packed, probs, key_capacity=1 << 20, device=self.device))
@@ -294,7 +297,7 @@ class BatchedSequenceTracker:
                 x, y, pol = (w.x, w.y, w.polarity) if hasattr(w, "x") else w[:3]
                 cam = None if hasattr(w, "x") else w[4]
                 mi, W, H, fx, fy = self.cameras[pi]
-                tt = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
+                tt = lambda a: a if torch.is_tensor(a) else torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
                 sig, uns = event_frames(tt(x), tt(y), tt(pol), W, H, 9, self.levels, self.device, camera=cam)
                 for l in range(self.levels):
                     self.ev[l][slot][0].copy_(sig[l].reshape(-1))

@@ -12,6 +12,7 @@ kernel of libgsevt.so.
 import ctypes as C
 import math
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -185,6 +186,11 @@ class GSFrame:
                 s.unsigned_mode = int(p.get("unsigned", False))
                 s.pose = int(p.get("pose", 0))
                 s.block_offset, s.num_blocks = lb_, nb
+                eps = p.get("log_eps")
+                if eps is not None:
+                    if not eps > 0:
+                        raise ValueError("log_eps must be positive, got %r" % (eps,))
+                    s.log_grey, s.log_eps = 1, float(eps)
                 pstructs.append(s)
             self.pair_table = _struct_tensor(pstructs, self.device)
         else:
@@ -237,6 +243,26 @@ class GSFrame:
             t = getattr(self, name)
             setattr(f, name, None if t is None else t.data_ptr())
         return f
+
+    def set_view_pose(self, i, R, t):
+        """Move host-filled view i to the world -> camera pose (R, t) (enqueued copy)."""
+        v = self.views[i]
+        v.R, v.t = R, t
+        v.campos = (-(np.asarray(R, np.float64).T @ np.asarray(t, np.float64))).tolist()
+        s = _lib.View.from_buffer_copy(bytes(self.view_table[i * C.sizeof(_lib.View):(i + 1) * C.sizeof(_lib.View)]
+                                             .cpu().numpy()))
+        for k in range(9):
+            s.R[k] = float(R[k // 3][k % 3])
+        for k in range(3):
+            s.t[k] = float(t[k])
+            s.campos[k] = float(v.campos[k])
+        raw = torch.frombuffer(bytearray(bytes(s)), dtype=torch.uint8)
+        self.view_table[i * C.sizeof(_lib.View):(i + 1) * C.sizeof(_lib.View)].copy_(raw)
+
+    def set_spin_limit(self, limit):
+        """Polls a bounded device wait makes before it gives up (0: the library default)."""
+        self.L.spin_limit = int(limit)
+        self._frame.L.spin_limit = int(limit)
 
     def grow(self, key_capacity):
         """Reallocate the workspace for a larger key capacity (contents are lost)."""
@@ -294,6 +320,8 @@ class GSFrame:
                 self.grow(int(k * 1.25) + 1024)
                 self.preprocess()
                 st, k = self.status()
+            if st & _lib.STATUS_SORT_TIMEOUT:
+                raise _lib.GsevtError("depth sort: %s" % _lib.status_names(st & _lib.STATUS_SORT_TIMEOUT))
             max_keys = max(k, 1)  # 0 would mean "size the sort grid from the capacity"
             self.num_keys = k
         self.bin_and_sort(max_keys)

@@ -129,3 +129,56 @@ def synth_events(I_last, I_next, n_events, seed, contrast=0.2, noise_frac=0.05, 
     perm = rng.permutation(idx.shape[0])
     idx, pol = idx[perm], pol[perm]
     return (idx % W).astype(np.uint16), (idx // W).astype(np.uint16), pol, ts
+
+
+class SinusoidTrajectory:
+    """Ground-truth motion of one synthetic sequence: T(tau) = exp(sin(2 pi f tau) zeta) with
+    zeta = [a_t u, a_r k] for unit axes u (translation) and k (rotation) drawn from the
+    seed, a_t = 0.5 m and a_r = 20 degrees at f = 0.2 Hz by default (world -> camera poses,
+    identity at tau = 0).  The path is a one-parameter subgroup, so the left twist rate
+    that the tracker's velocity model uses (T(tau + h) = exp(h [v, w]) T(tau)) is exactly
+    2 pi f cos(2 pi f tau) zeta."""
+
+    def __init__(self, seed, amp_m=0.5, amp_deg=20.0, freq_hz=0.2):
+        rng = np.random.default_rng(seed)
+        u = rng.normal(size=3)
+        k = rng.normal(size=3)
+        self.zeta = np.concatenate([amp_m * u / np.linalg.norm(u), math.radians(amp_deg) * k / np.linalg.norm(k)])
+        self.omega = 2.0 * math.pi * freq_hz
+
+    def pose(self, tau):
+        T = P.exp_se3(math.sin(self.omega * tau) * self.zeta)
+        return T[:3, :3].copy(), T[:3, 3].copy()
+
+    def velocity(self, tau):
+        """(linear, angular) twist rate at tau, in the tracker's convention."""
+        xi = self.omega * math.cos(self.omega * tau) * self.zeta
+        return xi[:3].copy(), xi[3:].copy()
+
+
+def synth_events_device(I_last, I_next, n_events, generator, contrast=0.2, noise_frac=0.05, eps=1e-3):
+    """Device form of synth_events for [H, W] torch images (same model: signal events
+    distributed over pixels in proportion to |ln(I_next + eps) - ln(I_last + eps)| / C,
+    polarity its sign, plus uniform noise events of random polarity), drawn with a torch
+    generator on the images' device.  Returns x, y (uint16 tensors) and polarity (uint8
+    tensor); event order is irrelevant to the event frame."""
+    import torch
+    H, W = I_last.shape
+    dl = (torch.log(I_next.double() + eps) - torch.log(I_last.double() + eps)).reshape(-1)
+    lam = dl.abs() / contrast
+    n_noise = int(round(n_events * noise_frac))
+    n_sig = n_events - n_noise
+    dev = I_last.device
+    if float(lam.sum()) > 0 and n_sig > 0:
+        idx = torch.multinomial(lam.float(), n_sig, replacement=True, generator=generator)
+        pol = (dl[idx] > 0).to(torch.uint8)
+    else:
+        idx = torch.zeros(0, dtype=torch.int64, device=dev)
+        pol = torch.zeros(0, dtype=torch.uint8, device=dev)
+        n_noise = n_events
+    nidx = torch.randint(0, H * W, (n_noise,), generator=generator, device=dev)
+    npol = torch.randint(0, 2, (n_noise,), generator=generator, device=dev).to(torch.uint8)
+    idx = torch.cat([idx, nidx])
+    pol = torch.cat([pol, npol])
+    # coordinates below 2^15: the int16 bits are the uint16 values
+    return (idx % W).to(torch.int16).view(torch.uint16), (idx // W).to(torch.int16).view(torch.uint16), pol

@@ -19,8 +19,12 @@ GREY_WEIGHTS = (0.2989, 0.5870, 0.1140)
 
 
 class RenderFrame:
-    def __init__(self, viewpoint, gaussians, pipeline, background, pyramid_level):
+    """log_eps: None for the reference's linear grey change (frame.py:86-92), or eps > 0
+    for the log-intensity change ln(I_next + eps) - ln(I_last + eps) of the paper."""
+
+    def __init__(self, viewpoint, gaussians, pipeline, background, pyramid_level, log_eps=None):
         self.viewpoint, self.gaussians, self.pipeline, self.background = viewpoint, gaussians, pipeline, background
+        self.log_eps = log_eps
         self.sign_delta_Ir, self.unsign_delta_Ir = self.get_delta_Ir(pyramid_level)
 
     @staticmethod
@@ -42,7 +46,10 @@ class RenderFrame:
             cams.append(Camera(T[:3, :3], T[:3, 3], vp.angular_vel, vp.linear_vel, focal2fov(vp.fx * s, w),
                                focal2fov(vp.fy * s, h), w, h, delta_tau=vp.delta_tau, device=vp.device))
         last_pkg, next_pkg = render2(cams[0], vp, cams[1], self.gaussians, self.background)
-        d = self.get_intensity_frame(next_pkg["render"]) - self.get_intensity_frame(last_pkg["render"])
+        In, Il = self.get_intensity_frame(next_pkg["render"]), self.get_intensity_frame(last_pkg["render"])
+        if self.log_eps:
+            In, Il = torch.log(In + self.log_eps), torch.log(Il + self.log_eps)
+        d = In - Il
         n = d / torch.norm(d, p=2)
         return n, torch.abs(n)
 
@@ -67,8 +74,9 @@ def make_optimizer(viewpoint, lrs):
 
 
 def plain_iteration(viewpoint, gaussians, background, optimizer, lvl, opt_vel, sign_Ie, unsign_Ie,
-                    lr_fraction=None, lrs=None, read_loss=True):
-    """One tracking iteration of the plain path (tracker.py:177-222)."""
+                    lr_fraction=None, lrs=None, read_loss=True, log_eps=None):
+    """One tracking iteration of the plain path (tracker.py:177-222); log_eps selects the
+    log-intensity change (RenderFrame)."""
     viewpoint.cam_w_delta.requires_grad_(bool(opt_vel))
     viewpoint.cam_v_delta.requires_grad_(bool(opt_vel))
     if opt_vel and lr_fraction is not None and lrs is not None:
@@ -76,7 +84,7 @@ def plain_iteration(viewpoint, gaussians, background, optimizer, lvl, opt_vel, s
         for g, name in zip(optimizer.param_groups, names):
             f = lr_fraction if name in ("cam_rot_delta", "cam_trans_delta") else 1 - lr_fraction
             g["lr"] = lrs[name] * f
-    rf = RenderFrame(viewpoint, gaussians, None, background, lvl)
+    rf = RenderFrame(viewpoint, gaussians, None, background, lvl, log_eps=log_eps)
     loss = tracking_loss(rf.sign_delta_Ir, sign_Ie) if opt_vel else tracking_loss(rf.unsign_delta_Ir, unsign_Ie)
     loss.backward()
     val = loss.item() if read_loss else loss.detach()
@@ -113,7 +121,10 @@ class Tracker:
         self.lrs = {k: opt[k] for k in ("cam_rot_delta", "cam_trans_delta", "cam_w_delta", "cam_v_delta")}
         self.pyramid_lvl = 3
         self.log = logging.getLogger("gsevt.tracker")
-        self.save_path = (config.get("Tracking") or {}).get("save_path") if hasattr(config, "get") else None
+        tracking_cfg = (config.get("Tracking") or {}) if hasattr(config, "get") else {}
+        self.save_path = tracking_cfg.get("save_path")
+        # optional (not a key of the reference's configs): eps of the log-intensity change
+        self.log_eps = tracking_cfg.get("log_grey_eps")
         self.trajectory = []
         self.iterations = 0
 
@@ -153,7 +164,8 @@ class Tracker:
                         k = it - start_vel
                         frac = k / fraction_num if 1 <= k <= fraction_num else 1
                     val, rf = plain_iteration(vp, self.gaussians, self.background, optimizer, lvl, opt_vel,
-                                              ef.sign_pyramid[lvl], ef.unsign_pyramid[lvl], frac, self.lrs)
+                                              ef.sign_pyramid[lvl], ef.unsign_pyramid[lvl], frac, self.lrs,
+                                              log_eps=self.log_eps)
                     self.iterations += 1
                     losses.append(val)
                     if self.check_convergence(losses, self.converged_threshold):

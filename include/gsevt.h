@@ -19,7 +19,12 @@
  *   - No entry point allocates device memory: scratch lives in the caller-provided
  *     workspace sized by gsevt_workspace_bytes (gsevt_events_accumulate_noalloc uses a
  *     fixed library-owned buffer instead; see its declaration).
- *   - Re-entrant per stream; no global mutable state other than that buffer.
+ *   - Re-entrant per stream.  Process-wide state: the cooperative sort's grid per device
+ *     (set once by gsevt_workspace_init), and the no-allocation event frame's fixed
+ *     buffer with its per-context address cache.
+ *   - Every entry point that enqueues work first clears a non-sticky CUDA error that an
+ *     earlier, unrelated call left pending, so that GSEVT_ERR_CUDA always refers to the
+ *     call's own launches and copies.
  */
 #ifndef GSEVT_H
 #define GSEVT_H
@@ -112,7 +117,10 @@ typedef struct gsevt_map_grads {
 } gsevt_map_grads;
 
 /* A (t, t + dtau) render pair and its event frame (utils/render_camera/frame.py:86-94,
- * utils/tracker.py:93-103). */
+ * utils/tracker.py:93-103).  The intensity change is dI = I_next - I_last of the grey
+ * renders (the reference's linear grey, frame.py:39-43,86-92), or with log_grey set the
+ * log-intensity change of the paper, dI = ln(I_next + log_eps) - ln(I_last + log_eps),
+ * applied per pixel after blending. */
 typedef struct gsevt_pair {
     int32_t last_view, next_view;
     const float *event;      /* [H][W] signed event frame E */
@@ -121,6 +129,8 @@ typedef struct gsevt_pair {
     int32_t pose;            /* pose state this pair belongs to (batched tracker) */
     int32_t block_offset;    /* first loss-reduction block of this pair */
     int32_t num_blocks;
+    int32_t log_grey;        /* 0: linear grey (default), 1: log grey */
+    float log_eps;           /* offset inside the logarithm (log_grey only), > 0 */
 } gsevt_pair;
 
 /* Sizes of one rendering frame (host struct). */
@@ -138,6 +148,13 @@ typedef struct gsevt_layout {
                                  * (the batched step's 4x4-tile super-tiles); 0: use the
                                  * bound total_tiles / 4 + num_views + 1, which can cost the
                                  * super-tile sort a second pass */
+    uint32_t spin_limit;        /* polls a bounded device wait (sort look-back, cooperative
+                                 * grid barrier) makes before it gives up and records
+                                 * GSEVT_STATUS_SORT_TIMEOUT; 0: the default, 2^22.  After a
+                                 * timeout the stages that follow the sort do nothing (no
+                                 * image, loss or pose update) until the status is cleared,
+                                 * which every gsevt_preprocess_fwd and
+                                 * gsevt_track_step_batched call does first. */
 } gsevt_layout;
 
 /* One rendering frame: layout, device tables, workspace and caller-owned outputs. */
@@ -256,12 +273,16 @@ int gsevt_events_accumulate(int64_t n, const uint16_t *x, const uint16_t *y,
  * turns each event packet into a frame and holds no device allocator, a host whose device
  * memory is all handed to its own pool, or a per-packet path that must not pay
  * cudaMalloc's implicit device synchronisation.
- *   - Scratch is one fixed library-owned buffer per device, sized for frames of up to
- *     GSEVT_EVENTS_NOALLOC_MAX_PIXELS pixels (1280 x 720; 14,747,648 bytes of device
- *     memory, taken when the library's event module loads on that device).  width *
- *     height above that returns GSEVT_ERR_TOO_LARGE before anything is enqueued.
- *   - Set-up: the first call on each device (with that device current) resolves the
- *     buffer's address with cudaGetSymbolAddress and caches it; make that first call
+ *   - Scratch is one fixed library-owned buffer per CUDA context, sized for frames of up
+ *     to GSEVT_EVENTS_NOALLOC_MAX_PIXELS pixels (1280 x 720; 14,747,648 bytes of device
+ *     memory, reserved when the library's event module is loaded into a context, which
+ *     under CUDA's default lazy module loading is its first use there, and held until
+ *     the context ends).  width * height above that returns GSEVT_ERR_TOO_LARGE before
+ *     anything is enqueued.
+ *   - Set-up: the first call in each context (a device's primary context, or a context
+ *     the caller created and made current) resolves the buffer's address there with
+ *     cudaGetSymbolAddress and caches it under the context's unique id, so a context
+ *     created later (after cudaDeviceReset, say) resolves its own; make that first call
  *     outside any stream capture.
  *   - The count image that must start at zero is cleared on the stream by every call;
  *     the other scratch regions are fully overwritten.

@@ -658,12 +658,22 @@ void or_frozen_backward_f64(int n, const float *xyz, const float *scale, const f
  * utils/tracker.py:93-103): dI = I_next - I_last; n = dI/||dI||;
  * signed: L = ||n - E||; unsigned: L = || |n| - |E| ||.  FP64 throughout.
  * Gradients dL/dI_next = -dL/dI_last written when non-NULL. */
+/* Pair loss of utils/tracker.py:93-103 over dI of utils/render_camera/frame.py:86-92,
+ * in FP64.  log_eps > 0 selects the log-intensity change dI = ln(I_next + eps) -
+ * ln(I_last + eps) (the image gradients then carry the factor 1 / (I + eps)); log_eps <= 0
+ * the reference's linear dI = I_next - I_last. */
+static double dI_at(const float *I_last, const float *I_next, int64_t i, double log_eps)
+{
+    if (log_eps > 0) return log((double)I_next[i] + log_eps) - log((double)I_last[i] + log_eps);
+    return (double)I_next[i] - (double)I_last[i];
+}
+
 double or_loss(int64_t npix, const float *I_last, const float *I_next, const float *E,
-               int unsigned_mode, double *dL_dnext, double *dL_dlast)
+               int unsigned_mode, double log_eps, double *dL_dnext, double *dL_dlast)
 {
     double s2 = 0, cross = 0, e2 = 0;
     for (int64_t i = 0; i < npix; ++i) {
-        double d = (double)I_next[i] - (double)I_last[i];
+        double d = dI_at(I_last, I_next, i, log_eps);
         double e = E[i];
         s2 += d * d;
         e2 += e * e;
@@ -675,7 +685,7 @@ double or_loss(int64_t npix, const float *I_last, const float *I_next, const flo
     if (dL_dnext || dL_dlast) {
         double ng = (1.0 - cross / s) / L;
         for (int64_t i = 0; i < npix; ++i) {
-            double d = (double)I_next[i] - (double)I_last[i];
+            double d = dI_at(I_last, I_next, i, log_eps);
             double n = d / s, e = E[i], g;
             if (unsigned_mode) {
                 double sg = (d > 0) - (d < 0);
@@ -684,8 +694,8 @@ double or_loss(int64_t npix, const float *I_last, const float *I_next, const flo
                 g = (n - e) / L;
             }
             double dd = (g - n * ng) / s;
-            if (dL_dnext) dL_dnext[i] = dd;
-            if (dL_dlast) dL_dlast[i] = -dd;
+            if (dL_dnext) dL_dnext[i] = log_eps > 0 ? dd / ((double)I_next[i] + log_eps) : dd;
+            if (dL_dlast) dL_dlast[i] = log_eps > 0 ? -dd / ((double)I_last[i] + log_eps) : -dd;
         }
     }
     return L;

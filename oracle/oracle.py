@@ -69,7 +69,7 @@ def lib():
                                              _opt(f64p), _opt(f64p), _opt(f64p), _opt(f64p),
                                              _opt(f64p), _opt(f64p)]
         L.or_loss.restype = C.c_double
-        L.or_loss.argtypes = [C.c_int64, f32p, f32p, f32p, C.c_int, _opt(f64p), _opt(f64p)]
+        L.or_loss.argtypes = [C.c_int64, f32p, f32p, f32p, C.c_int, C.c_double, _opt(f64p), _opt(f64p)]
         L.or_event_frame.argtypes = [C.c_int, C.c_int, C.c_int64, u16p, u16p, u8p, C.c_int, _opt(f64p),
                                      f32p, _opt(f32p), _opt(i32p)]
         L.or_undistort.argtypes = [f32p, C.c_int, C.c_int, f64p, f32p]
@@ -233,18 +233,24 @@ def frozen_backward(rec, xyz, opac, view64, W, H, bg, nch, dL_dout, sh=None, sca
     return g_xi, mg
 
 
-def loss(I_last, I_next, E, unsigned=False, grads=False):
+def loss(I_last, I_next, E, unsigned=False, grads=False, log_eps=None):
+    """Pair loss (FP64) of two grey renders against the event frame; log_eps selects the
+    log-intensity change ln(I + eps) instead of the linear one."""
     I_last, I_next, E = _c(I_last, np.float32), _c(I_next, np.float32), _c(E, np.float32)
     n = I_last.size
     gn = np.zeros(n, np.float64) if grads else None
     gl = np.zeros(n, np.float64) if grads else None
-    L = lib().or_loss(n, I_last.reshape(-1), I_next.reshape(-1), E.reshape(-1), int(unsigned), gn, gl)
+    L = lib().or_loss(n, I_last.reshape(-1), I_next.reshape(-1), E.reshape(-1), int(unsigned),
+                      float(log_eps) if log_eps else -1.0, gn, gl)
     return (L, gn, gl) if grads else L
 
 
-def loss_f64(I_last, I_next, E, unsigned=False):
+def loss_f64(I_last, I_next, E, unsigned=False, log_eps=None):
     """Same loss evaluated from FP64 images (numpy), for finite differences."""
-    d = np.asarray(I_next, np.float64) - np.asarray(I_last, np.float64)
+    if log_eps:
+        d = np.log(np.asarray(I_next, np.float64) + log_eps) - np.log(np.asarray(I_last, np.float64) + log_eps)
+    else:
+        d = np.asarray(I_next, np.float64) - np.asarray(I_last, np.float64)
     n = d / np.sqrt(np.sum(d * d))
     E = np.asarray(E, np.float64)
     r = (np.abs(n) - np.abs(E)) if unsigned else (n - E)

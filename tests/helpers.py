@@ -42,7 +42,7 @@ def pair_views(R, t, lin, ang, dtau):
     return (Tl[:3, :3], Tl[:3, 3]), (Tn[:3, :3], Tn[:3, 3])
 
 
-def oracle_pair_loss_f64(m, cam, R, t, lin, ang, dtau, E, recs, unsigned=False, cov=None):
+def oracle_pair_loss_f64(m, cam, R, t, lin, ang, dtau, E, recs, unsigned=False, cov=None, log_eps=None):
     """FP64 frozen pair loss for pose (R, t) and velocity (lin, ang)."""
     from oracle import oracle
     (Rl, tl), (Rn, tn) = pair_views(R, t, lin, ang, dtau)
@@ -53,4 +53,4 @@ def oracle_pair_loss_f64(m, cam, R, t, lin, ang, dtau, E, recs, unsigned=False, 
                                          sh=m["sh"], cov_pre=cov, scale=None if cov is not None else m["scale"],
                                          rot=None if cov is not None else m["rot"])
         imgs.append(out[0])
-    return oracle.loss_f64(imgs[0], imgs[1], E, unsigned)
+    return oracle.loss_f64(imgs[0], imgs[1], E, unsigned, log_eps=log_eps)

@@ -60,6 +60,11 @@ def test_argument_validation_without_gpu():
     assert L.gsevt_events_accumulate(10, None, None, None, 64, 48, None, 9, 3, None, None, None, None) == -1
     assert L.gsevt_events_accumulate(0, None, None, None, 64, 48, None, 8, 1, C.c_void_p(16), C.c_void_p(16),
                                      None, None) == -1  # even kernel size
+    # a camera with fx = 0 is rejected before anything is enqueued (the fake pointers are
+    # never touched)
+    cam = (C.c_double * 9)(0.0, 300.0, 32.0, 24.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    assert L.gsevt_events_accumulate(0, None, None, None, 64, 48, cam, 9, 1, C.c_void_p(16), C.c_void_p(16),
+                                     None, None) == -1
     assert L.gsevt_pack_map(10, None, None, None, None, None, None, 16, 1.0, None, None) == -1
     assert L.gsevt_chain_view_grad(None, None, 0.0, None, None, None, None) == -1
 

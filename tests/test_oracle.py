@@ -121,6 +121,38 @@ def test_grey_normalisation_loss_golden():
     assert abs(oracle.loss(gl, gn, np.abs(E), True) - float(GOLD["loss_unsigned"])) < 1e-5
 
 
+@pytest.mark.parametrize("unsigned", [False, True])
+def test_log_grey_loss_and_image_gradients(unsigned):
+    """Log-intensity mode of the pair loss (dI = ln(I_next + eps) - ln(I_last + eps)): the C
+    oracle equals the numpy FP64 form, and its image gradients (which carry 1 / (I + eps))
+    match central finite differences; eps -> 0 is not taken, and without log_eps the
+    linear form is unchanged."""
+    rng = np.random.default_rng(9)
+    H, W, eps = 12, 16, 1e-3
+    Il = rng.uniform(0.0, 1.0, (H, W)).astype(np.float32)
+    In = (Il + rng.normal(0.0, 0.05, (H, W))).clip(0.0, None).astype(np.float32)
+    E = rng.normal(size=(H, W)).astype(np.float32)
+    E /= np.linalg.norm(E.astype(np.float64))
+    if unsigned:
+        E = np.abs(E)
+    L, gn, gl = oracle.loss(Il, In, E, unsigned, grads=True, log_eps=eps)
+    assert abs(L - oracle.loss_f64(Il, In, E, unsigned, log_eps=eps)) < 1e-12
+    assert abs(oracle.loss(Il, In, E, unsigned) - oracle.loss_f64(Il, In, E, unsigned)) < 1e-12
+    assert abs(L - oracle.loss(Il, In, E, unsigned)) > 1e-3  # the two modes differ
+    h = 1e-7
+    for k in rng.choice(H * W, 12, replace=False):
+        for img, g in ((In, gn), (Il, gl)):
+            a = img.astype(np.float64).copy()
+            b = a.copy()
+            a.reshape(-1)[k] += h
+            b.reshape(-1)[k] -= h
+            args = (a, In.astype(np.float64)) if img is Il else (Il.astype(np.float64), a)
+            argsb = (b, In.astype(np.float64)) if img is Il else (Il.astype(np.float64), b)
+            fd = (oracle.loss_f64(*args, E, unsigned, log_eps=eps) - oracle.loss_f64(*argsb, E, unsigned,
+                                                                                      log_eps=eps)) / (2 * h)
+            assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(fd)), (k, fd, g[k])
+
+
 def test_convergence_golden():
     from gsevt.tracker import check_convergence
     L = list(GOLD["conv_losses"])

@@ -1,8 +1,9 @@
 """gsevt_events_accumulate_noalloc (scratch in a fixed library-owned device buffer, no
 allocation) against gsevt_events_accumulate (caller scratch), both called through the
 C ABI.  Two calls in a row on different event packets check that the second call starts
-from a cleared count image.  Kept in a file of its own that runs last, so it also runs
-after every other test has loaded and used the library."""
+from a cleared count image; the outputs must be equal bit for bit.  Kept in a file of its
+own that runs last, so it also runs after every other test has loaded and used the
+library."""
 import ctypes as C
 
 import numpy as np
@@ -75,6 +76,8 @@ def test_noalloc_matches_caller_scratch_entry_point(W, H, camera):
         torch.cuda.synchronize()
         a, b = out_s.cpu().numpy(), ref_s.cpu().numpy()
         assert np.isfinite(a).all() and np.abs(b).max() > 0, call
-        # same kernels and launch shapes over the same inputs: equal to FP32 rounding
-        np.testing.assert_allclose(a, b, rtol=0, atol=1e-7, err_msg="call %d" % call)
-        np.testing.assert_allclose(out_u.cpu().numpy(), np.abs(b), rtol=0, atol=1e-7, err_msg="call %d" % call)
+        # the same launch sequence over the same inputs is deterministic (integer atomics,
+        # fixed-order FP64 partials): the outputs are equal bit for bit
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), "call %d" % call
+        u = out_u.cpu().numpy()
+        assert np.array_equal(u.view(np.uint32), np.abs(b).view(np.uint32)), "call %d" % call
