@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     const gsevt_pair pr = pairs[pi];
     const gsevt_view &Vl = views[pr.last_view];
     const gsevt_view &Vn = views[pr.next_view];
+    if (Vl.skip || Vn.skip) return;  // a finished problem: nothing rendered (uniform per pair)
     const int P = Vl.width * Vl.height;
     const int lb = b - pr.block_offset;
     // FP32 sums over this thread's 8 pixels, FP64 from the warp level up

@@ -339,7 +339,8 @@ __global__ void __launch_bounds__(GS_BLOCK, 2) k_preprocess_fwd(FwdParams p)
         uint32_t touched = 0;
         if (valid) {
             Pre o;
-            bool vis = pre_forward(a.xyz, a.cov, a.sh, M.sh_degree, a.has_col ? a.col : nullptr, V, o);
+            // a skipped view (a finished tracking problem) culls every Gaussian
+            bool vis = !V.skip && pre_forward(a.xyz, a.cov, a.sh, M.sh_degree, a.has_col ? a.col : nullptr, V, o);
             size_t vg = (size_t)V.vg_offset + g;
             if (vis && p.ws.fcache) tighten_rect(o, a.opac, V);
             vis = vis && o.rect[2] > o.rect[0] && o.rect[3] > o.rect[1];

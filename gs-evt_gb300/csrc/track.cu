@@ -404,6 +404,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
             float tE[3];
             pair_pose(S, sg[lane], Rs, ts, RE, tE);
             write_view_pose(views + vids[lane], Rs, ts);
+            // a problem whose level just finished renders nothing until the host resets it
+            views[vids[lane]].skip = (S.control && S.frozen) ? 1 : 0;
         }
     }
     __syncwarp();
@@ -424,6 +426,7 @@ __global__ void k_track_views(gsevt_view *views, const gsevt_pose_state *poses, 
         float tE[3];
         pair_pose(S, sg[k], Rs, ts, RE, tE);
         write_view_pose(views + vids[k], Rs, ts);
+        views[vids[k]].skip = (S.control && S.frozen) ? 1 : 0;
     }
 }
 
@@ -474,7 +477,7 @@ __global__ void k_view_from_settings(const float *vm_t, const float *pr_t, const
     V.sb_offset = sb_offset;
     V.pair = -1;
     V.pair_role = 0;
-    V.pad = 0;
+    V.skip = 0;
     *out = V;
 }
 

@@ -53,7 +53,7 @@ class View(C.Structure):
                 ("tiles_x", C.c_int32), ("tiles_y", C.c_int32), ("tile_offset", C.c_int32),
                 ("pix_offset", C.c_int32), ("map", C.c_int32), ("vg_offset", C.c_int32),
                 ("sb_offset", C.c_int32), ("pair", C.c_int32), ("pair_role", C.c_int32),
-                ("pad", C.c_int32)]
+                ("skip", C.c_int32)]
 
 
 class Map(C.Structure):

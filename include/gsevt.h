@@ -77,7 +77,9 @@ typedef struct gsevt_view {
     int32_t sb_offset;    /* first scan block of this view */
     int32_t pair;         /* render pair this view belongs to, or -1 */
     int32_t pair_role;    /* 0: t (last), 1: t + dtau (next) */
-    int32_t pad;
+    int32_t skip;         /* 1: render nothing for this view (every Gaussian is culled); the
+                           * batched step sets it for the views of a problem whose pyramid
+                           * level has finished, gsevt_track_init_views clears it */
 } gsevt_view;
 
 /* One Gaussian map (device-resident table entry).  Exactly one colour source
