@@ -202,7 +202,7 @@ def build_problem(name, device, seed_offset=0):
                 E_unsigned=uns[0].reshape(-1).contiguous(), events=(ex, ey, ep, ts), hypotheses=hyp)
 
 
-def make_tracker(prob, device, hypotheses=None):
+def make_tracker(prob, device, hypotheses=None, tuning="table"):
     from gsevt import synthetic
     from gsevt.batched import BatchedTracker, Problem
     sc = prob["scenario"]
@@ -215,7 +215,7 @@ def make_tracker(prob, device, hypotheses=None):
     own = (lambda t: t.clone()) if hyp > 1 else (lambda t: t)
     probs = [Problem(0, R, t, sc.init_lin, sc.init_ang, sc.delta_tau, prob["W"], prob["H"], prob["f"], prob["f"],
                      own(prob["E"]), own(prob["E_unsigned"]), opt_vel=True) for R, t in poses]
-    return BatchedTracker([{"packed": prob["packed"], "n": prob["n"]}], probs, device=device)
+    return BatchedTracker([{"packed": prob["packed"], "n": prob["n"]}], probs, device=device, tuning=tuning)
 
 
 def time_graph(bt, steps, warmup, flush):
@@ -253,13 +253,15 @@ def run_hypotheses(dev, flush, steps=10, warmup=3):
             "problem_iters_per_s": 1000.0 / ms * bt.num, "keys": int(bt.num_keys),
             "iterations_run": int(st["iter"][0]), "best_hypothesis_error_mm": 1000.0 * err_t[best],
             "best_hypothesis_error_deg": err_r[best],
-            "l2": "flushed (256 MB write) between timed iterations"}
+            "l2": "flushed (256 MB write) between timed iterations",
+            "tuning": dict(bt.frame.tuning(), source=bt.tuning_source)}
 
 
-def run_sequences(dev, flush, steps=10, warmup=3, count=16):
+def make_sequences_tracker(dev, count=16, tuning="table"):
     """16 concurrent sequences, each with its own map (log-uniform 50k-1.5M Gaussians,
     seeds 10-25) and resolution (346x260, 640x480, 1280x720 in turn), event windows of
-    log-uniform 10k-2M events, all views in one launch per stage."""
+    log-uniform 10k-2M events, all views in one launch per stage.  Returns (tracker,
+    total Gaussians, resolutions)."""
     import torch
     from gsevt import synthetic
     from gsevt import pose as gpose
@@ -291,11 +293,17 @@ def run_sequences(dev, flush, steps=10, warmup=3, count=16):
         probs.append(Problem(i, sc.init_R, sc.init_t, sc.init_lin, sc.init_ang, sc.delta_tau, W, H, f, f,
                              sig[0].reshape(-1).contiguous(), uns[0].reshape(-1).contiguous(), opt_vel=True))
         total += n
-    bt = BatchedTracker(maps, probs, device=dev)
+    return BatchedTracker(maps, probs, device=dev, tuning=tuning), total, res
+
+
+def run_sequences(dev, flush, steps=10, warmup=3, count=16):
+    """The 16 uneven sequences of make_sequences_tracker: time of one iteration of all."""
+    bt, total, res = make_sequences_tracker(dev, count)
     ms = time_graph(bt, steps, warmup, flush)
     return {"workload": "sequences-16-uneven", "problems": count, "views": 2 * count, "gaussians_total": total,
             "ms_per_iter": ms, "problem_iters_per_s": 1000.0 / ms * count, "keys": int(bt.num_keys),
-            "resolutions": ["%dx%d" % r for r in res], "l2": "flushed (256 MB write) between timed iterations"}
+            "resolutions": ["%dx%d" % r for r in res], "l2": "flushed (256 MB write) between timed iterations",
+            "tuning": dict(bt.frame.tuning(), source=bt.tuning_source)}
 
 
 def run_sequence_tracking(dev, frames=10, count=16, window_s=0.025):
@@ -380,6 +388,30 @@ def run_sequence_tracking(dev, frames=10, count=16, window_s=0.025):
             "mean_rms_drift_mm": 1e3 * float(np.mean(drift_t)), "mean_rms_drift_deg": float(np.mean(drift_r)),
             "final_error_mm": [1e3 * v for v in final_t],
             "trajectory": "T(tau) = exp(sin(2 pi 0.2 tau) [0.5 m u, 20 deg k]), u, k unit axes per sequence"}
+
+
+def tune_workloads(names, iters=20, out=None):
+    """Autotune the launch choices of each named workload on this GPU (gsevt.tuner) and
+    write the table; prints one JSON line per workload."""
+    import torch
+    from gsevt import tuner
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    table = tuner.load_table(out or tuner.TABLE_PATH)
+    for name in names:
+        if name == "sequences-16-uneven":
+            bt, _, _ = make_sequences_tracker(dev, tuning="defaults")
+        else:
+            bt = make_tracker(build_problem(name, dev), dev, tuning="defaults")
+        best, ms, trials = tuner.tune(bt, iters=iters, flush=flush)
+        tuner.record(table, bt.frame.L, best, ms, trials, workload=name,
+                     device=torch.cuda.get_device_name(dev))
+        tuner.save_table(table, out or tuner.TABLE_PATH)
+        print(json.dumps({"mode": "tune", "workload": name, "key": tuner.shape_key(bt.frame.L), "choice": best,
+                          "ms_per_iter": ms, "trials": [{"choice": c, "ms": t} for c, t in trials]}))
+        del bt
+        torch.cuda.empty_cache()
 
 
 def stage_times(bt, reps=5):
@@ -686,7 +718,10 @@ def main():
                     help="skip the 64-hypothesis and 16-sequence workloads reported beside the headline")
     ap.add_argument("--sequence-frames", type=int, default=10,
                     help="frames each of the 16 sequences tracks in the sequence-tracking workload")
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "sequence-tracking"],
+    ap.add_argument("--tune-workload", action="append", default=None,
+                    help="with --mode tune: workloads to tune (default: the headline, the 64 hypotheses and "
+                         "the 16 sequences)")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "sequence-tracking", "tune"],
                     help="profile: build the workload, then run warmup + steps un-graphed iterations "
                          "(for ncu launch lists; prints no timings)")
     args = ap.parse_args()
@@ -694,6 +729,9 @@ def main():
         return run_reference(args)
     if args.mode == "profile":
         return run_profile(args)
+    if args.mode == "tune":
+        return tune_workloads(args.tune_workload or ["adjoint-500k-640x480", "hypotheses-64x2-500k",
+                                                     "sequences-16-uneven"])
     if args.mode == "sequence-tracking":
         import torch
         torch.cuda.set_device(0)
@@ -768,7 +806,8 @@ def main():
         "config": {"workload": args.workload, "gaussians": prob["n"], "width": prob["W"], "height": prob["H"],
                    "events": WORKLOADS[args.workload][5], "hypotheses": bt.num, "views_per_launch": 2 * bt.num,
                    "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "flushed (256 MB write) between timed iterations", "path": "batched adjoint, CUDA graph"},
+                   "l2": "flushed (256 MB write) between timed iterations", "path": "batched adjoint, CUDA graph",
+                   "tuning": dict(bt.frame.tuning(), source=bt.tuning_source)},
         "e2e": {"value": 1000.0 / e2e_ms * bt.num * world, "unit": "iters/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "plain": None if plain_ms is None else {"value": 1000.0 / plain_ms, "unit": "iters/s", "ms_per_step": plain_ms,

@@ -560,7 +560,7 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
     // the cooperative sort compacts the visible slots in its first pass; otherwise the
     // visible-slot scan and compaction kernels run first
     GsCompact cmp = {};
-    const bool fuse_compact = gs_coop_depth_sort((uint32_t)L.num_vg, (uint32_t)L.num_scan_blocks);
+    const bool fuse_compact = ws.coop_ok && gs_coop_depth_sort((uint32_t)L.num_vg, (uint32_t)L.num_scan_blocks);
     if (fuse_compact) {
         cmp.views = f->views;
         cmp.num_views = L.num_views;
@@ -624,7 +624,7 @@ int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, 
     uint32_t *k[2] = {ws.keys[0], ws.keys[1]};
     uint32_t *v[2] = {ws.vals[0], ws.vals[1]};
     int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 1, L.key_capacity, gs_tile_bits(L), max_keys,
-                                       GS_SORT_KPT_TILES, ws, &buf, s, nullptr, 0);
+                                       ws.pair_kpt, ws, &buf, s, nullptr, 0);
     if (st) return st;
     if (buf != gs_tile_sort_buffer(L)) return GSEVT_ERR_ARG;
     int blocks = (int)std::min<uint32_t>((max_keys + 255) / 256, 152u * 16u);
@@ -668,7 +668,7 @@ int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max
     int buf = 0;
     uint32_t *k[2] = {ws.keys[0], ws.keys[1]};
     uint32_t *v[2] = {ws.vals[0], ws.vals[1]};
-    int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 6, L.key_capacity, bits, max_keys, GS_SORT_KPT_TILES, ws,
+    int st = gs_launch_sort_t<uint32_t>(k, v, ws.status + 6, L.key_capacity, bits, max_keys, ws.pair_kpt, ws,
                                         &buf, s, one_pass ? ws.sranges : nullptr, one_pass ? nsup : 0u);
     if (st) return st;
     if (!one_pass) {

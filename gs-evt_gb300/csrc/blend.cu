@@ -31,6 +31,19 @@
 // both cannot pass the per-pixel alpha test, so the decisions and results are unchanged.
 // Every lane evaluates each candidate; the per-pixel decisions are predicates, not
 // divergent branches.
+//
+// Staging (gsevt_tuning.blend_staging): either every thread copies its candidate's 32-byte
+// record with two 16-byte cp.async, or (the grey tracker blends, staging 2) one warp stages
+// the whole batch with TMA: the records form a 2-D tensor of num_vg rows of 8 floats, and
+// each cp.async.bulk.tensor ... tile::gather4 copies four rows chosen by slot id into one
+// 128-byte aligned group of the batch buffer, completing on the buffer's mbarrier (every
+// wait on it is bounded; one that runs out sets GSEVT_STATUS_STAGE_TIMEOUT, and a block
+// that stops early still waits, again bounded, for the copies it issued).
+#include <cuda.h>
+
+#include <atomic>
+#include <cstring>
+
 #include "common.cuh"
 
 namespace {
@@ -57,9 +70,14 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-template <bool RGB> struct Batch {
-    float4 A[GS_BLOCK];
-    float4 B[GS_BLOCK];
+// One staged Gaussian: the slot's 32-byte blend record.
+struct Rec {
+    float4 A;  // {mean x, mean y, depth, grey}
+    float4 B;  // {conic x, y, z, opacity}
+};
+
+template <bool RGB> struct alignas(128) Batch {
+    Rec r[GS_BLOCK];  // first member: 128-byte aligned for the tensor-copy groups
     float4 C[RGB ? GS_BLOCK : 1];
     float4 box[GS_BLOCK];  // {xmin, xmax, ymin, ymax}: outside it the Gaussian fails the alpha test
     float4 ell[GS_BLOCK];  // {a, b, c, -tau}: quadratic form of the alpha support and its bound
@@ -128,7 +146,7 @@ __device__ __forceinline__ bool warp_hit(const Batch<RGB> &cur, int c0, int n, i
                                          float sy0, float sy1)
 {
     const int ci = min(c0 + lane, n - 1);
-    const float4 bx = cur.box[ci], A = cur.A[ci];
+    const float4 bx = cur.box[ci], A = cur.r[ci].A;
     const bool box = bx.y >= sx0 && bx.x <= sx1 && bx.w >= sy0 && bx.z <= sy1;
     const bool ell = ellipse_hits(A.x, A.y, cur.ell[ci], sx0, sx1, sy0, sy1);
     return (c0 + lane < n) & box & ell;
@@ -142,11 +160,94 @@ __device__ __forceinline__ void load_batch(const BlendParams &p, Batch<RGB> &buf
     if (idx < range.y) {
         uint32_t vg = __ldg(p.vals + idx);
         buf.id[threadIdx.x] = vg;
-        cp_async16(&buf.A[threadIdx.x], p.ws.recA + vg);
-        cp_async16(&buf.B[threadIdx.x], p.ws.recB + vg);
+        cp_async16(&buf.r[threadIdx.x].A, p.ws.rec + 2 * (size_t)vg);
+        cp_async16(&buf.r[threadIdx.x].B, p.ws.rec + 2 * (size_t)vg + 1);
         if (RGB) cp_async16(&buf.C[threadIdx.x], p.ws.recC + vg);
     }
     cp_async_commit();
+}
+
+// ---- TMA staging ----
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *m)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(m)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t *m, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(m)), "r"(bytes) : "memory");
+}
+
+// Bounded wait for the phase of parity `parity` to complete; false when `limit` polls ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *m, uint32_t parity, uint32_t limit)
+{
+    const uint32_t a = smem_addr(m);
+    for (uint32_t i = 0; i <= limit; ++i) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Four rows (r0..r3) of the 2-D record tensor, x = 0, into 128 contiguous bytes at dst.
+__device__ __forceinline__ void tma_gather4(void *dst, const CUtensorMap *tm, uint32_t r0, uint32_t r1, uint32_t r2,
+                                            uint32_t r3, uint64_t *m)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cta.global.tile::gather4.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                 ::"r"(smem_addr(dst)), "l"(tm), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_addr(m))
+                 : "memory");
+}
+
+// Warp 0 stages batch r of the tile range into buf: lane l takes the groups g = l and l + 32
+// of four candidates, reads their slot ids, stores them in buf.id, and (after lane 0 has
+// announced the batch's bytes on the mbarrier) copies their four records with one gather4
+// into the 128-byte group buf.r[4g .. 4g + 3].  Rows past the range repeat the batch's
+// first slot (copied but never read).  Called by all 32 lanes of warp 0.
+template <bool RGB>
+__device__ __forceinline__ void tma_load_batch(const BlendParams &p, Batch<RGB> &buf, uint2 range, int r,
+                                               uint64_t *mbar, const CUtensorMap *tm)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t base = range.x + (uint32_t)r * GS_BLOCK;
+    const uint32_t n = min((uint32_t)GS_BLOCK, range.y - base);  // >= 1
+    const uint32_t groups = (n + 3) / 4;
+    const uint32_t first = __ldg(p.vals + base);
+    uint32_t rows[2][4];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t c = 4 * (uint32_t)(lane + 32 * h) + (uint32_t)k;
+            rows[h][k] = c < n ? __ldg(p.vals + base + c) : first;
+            if (c < n) buf.id[c] = rows[h][k];
+        }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive_expect(mbar, groups * 128u);
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t g = (uint32_t)(lane + 32 * h);
+        if (g < groups) tma_gather4(&buf.r[4 * g], tm, rows[h][0], rows[h][1], rows[h][2], rows[h][3], mbar);
+    }
+}
+
+// Before a block exits: wait (bounded) for the batch it issued but did not consume (at
+// most one, batch `waited`, when the block stopped early), so that no tensor copy still
+// targets its shared memory.
+__device__ __forceinline__ void tma_drain(uint64_t *mbar, uint32_t phase, int issued, int waited, uint32_t limit,
+                                          uint32_t *status)
+{
+    if (issued > waited) {
+        const int b = waited & 1;
+        if (!mbar_wait(&mbar[b], (phase >> b) & 1u, limit) && threadIdx.x == 0)
+            atomicOr(status, GSEVT_STATUS_STAGE_TIMEOUT);
+    }
 }
 
 // Pixel of thread t: warps tile the 16x16 tile as 2 x 4 blocks of 8x4 pixels, so a warp's
@@ -173,7 +274,7 @@ __device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const Blend
                                               float pyf, float &T, float &C0, float &C1, float &C2, float &D,
                                               float &Aacc, int &last, bool &done)
 {
-    const float4 A = cur.A[j], B = cur.B[j];
+    const float4 A = cur.r[j].A, B = cur.r[j].B;
     const float dx = A.x - pxf, dy = A.y - pyf;
     const float power = gs_power(B.x, B.y, B.z, dx, dy);
     const float alpha = fminf(0.99f, B.w * gs_expf(power));
@@ -202,14 +303,22 @@ __device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const Blend
 // EXTRAS: the frame wants depth, alpha, contributor counts or n_touched (each still
 // checked at run time); without it only the image and the final transmittance are
 // accumulated (the batched tracker's case).
-template <bool EXTRAS, bool RGB>
-__global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams p)
+template <bool EXTRAS, bool RGB, bool TMA>
+__global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams p, const __grid_constant__ CUtensorMap tm)
 {
     __shared__ Batch<RGB> sb[2];
     __shared__ gsevt_view V;
+    __shared__ __align__(8) uint64_t mbar[2];
     const int tile = blockIdx.x;
     if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
-    if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
+    if (threadIdx.x == 0) {
+        V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
+        if (TMA) {
+            mbar_init(&mbar[0]);
+            mbar_init(&mbar[1]);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+    }
     __syncthreads();
     const int lt = tile - V.tile_offset;
     const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
@@ -225,10 +334,28 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
     int last = 0;
     bool done = !inside;
     const int lane = threadIdx.x & 31;
-    if (rounds > 0) load_batch(p, sb[0], range, 0);
+    uint32_t phase = 0;  // TMA: parity of the next phase of each buffer's mbarrier (bit b)
+    int issued = 0, waited = 0;  // TMA: batches issued / waited for
+    if (rounds > 0) {
+        if (TMA) {
+            if (threadIdx.x < 32) tma_load_batch(p, sb[0], range, 0, &mbar[0], &tm);
+            issued = 1;
+        } else {
+            load_batch(p, sb[0], range, 0);
+        }
+    }
     for (int r = 0; r < rounds; ++r) {
         Batch<RGB> &cur = sb[r & 1];
-        if (r + 1 < rounds) {
+        if (TMA) {
+            if (r + 1 < rounds) {
+                if (threadIdx.x < 32) tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], &tm);
+                issued = r + 2;
+            }
+            if (!mbar_wait(&mbar[r & 1], (phase >> (r & 1)) & 1u, p.ws.spin_limit) && threadIdx.x == 0)
+                atomicOr(p.ws.status, GSEVT_STATUS_STAGE_TIMEOUT);
+            phase ^= 1u << (r & 1);
+            waited = r + 1;
+        } else if (r + 1 < rounds) {
             load_batch(p, sb[(r + 1) & 1], range, r + 1);
             cp_async_wait<1>();
         } else {
@@ -238,7 +365,7 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
         if ((int)threadIdx.x < n) {
             float4 e;
-            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &e);
+            cur.box[threadIdx.x] = gauss_box(cur.r[threadIdx.x].A, cur.r[threadIdx.x].B, &e);
             cur.ell[threadIdx.x] = e;
         }
         __syncthreads();
@@ -261,7 +388,11 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
         }
         __syncthreads();  // the next iteration overwrites this buffer
     }
-    cp_async_wait<0>();  // no copy may still target shared memory when the block exits
+    if (TMA) {
+        tma_drain(mbar, phase, issued, waited, p.ws.spin_limit, p.ws.status);
+    } else {
+        cp_async_wait<0>();  // no copy may still target shared memory when the block exits
+    }
     if (inside) {
         const int pix = V.pix_offset + py * V.width + px;
         const size_t P = (size_t)p.total_pixels;
@@ -328,7 +459,7 @@ __device__ __forceinline__ float warp_reduce_transposed(float (&v)[NV], int lane
 __device__ __forceinline__ bool tracker_candidate(const Batch<false> &cur, int j, float pxf, float pyf, float Cimg,
                                                   float gC, float &T, float &Pc, bool &done, float (&g)[6])
 {
-    const float4 A = cur.A[j], B = cur.B[j];
+    const float4 A = cur.r[j].A, B = cur.r[j].B;
     const float dx = A.x - pxf, dy = A.y - pyf;
     const float power = gs_power(B.x, B.y, B.z, dx, dy);
     const float araw = B.w * gs_expf(power);
@@ -393,17 +524,25 @@ __device__ __forceinline__ float warp_reduce_pair6(const float (&a)[6], const fl
     return v[0];
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
+template <int MODE, bool TMA>
+__global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p, const __grid_constant__ CUtensorMap tm)
 {
     constexpr bool RGB = MODE == 2;
     constexpr int NC = Comps<MODE>::n;
     __shared__ Batch<RGB> sb[2];
     __shared__ float acc[GS_BLOCK][NC + 1];
     __shared__ gsevt_view V;
+    __shared__ __align__(8) uint64_t mbar[2];
     const int tile = blockIdx.x;
     if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
-    if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
+    if (threadIdx.x == 0) {
+        V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
+        if (TMA) {
+            mbar_init(&mbar[0]);
+            mbar_init(&mbar[1]);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+    }
     for (int i = threadIdx.x; i < GS_BLOCK * (NC + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -462,10 +601,28 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
 
     float T = 1.0f, Pc[3] = {0, 0, 0}, PD = 0.0f, PA = 0.0f;
     bool done = !inside;
-    if (rounds > 0) load_batch(p, sb[0], range, 0);
+    uint32_t phase = 0;  // TMA: parity of the next phase of each buffer's mbarrier (bit b)
+    int issued = 0, waited = 0;  // TMA: batches issued / waited for
+    if (rounds > 0) {
+        if (TMA) {
+            if (threadIdx.x < 32) tma_load_batch(p, sb[0], range, 0, &mbar[0], &tm);
+            issued = 1;
+        } else {
+            load_batch(p, sb[0], range, 0);
+        }
+    }
     for (int r = 0; r < rounds; ++r) {
         Batch<RGB> &cur = sb[r & 1];
-        if (r + 1 < rounds) {
+        if (TMA) {
+            if (r + 1 < rounds) {
+                if (threadIdx.x < 32) tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], &tm);
+                issued = r + 2;
+            }
+            if (!mbar_wait(&mbar[r & 1], (phase >> (r & 1)) & 1u, p.ws.spin_limit) && threadIdx.x == 0)
+                atomicOr(p.ws.status, GSEVT_STATUS_STAGE_TIMEOUT);
+            phase ^= 1u << (r & 1);
+            waited = r + 1;
+        } else if (r + 1 < rounds) {
             load_batch(p, sb[(r + 1) & 1], range, r + 1);
             cp_async_wait<1>();
         } else {
@@ -475,7 +632,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         const int n = min(GS_BLOCK, todo - r * GS_BLOCK);
         if ((int)threadIdx.x < n) {
             float4 e;
-            cur.box[threadIdx.x] = gauss_box(cur.A[threadIdx.x], cur.B[threadIdx.x], &e);
+            cur.box[threadIdx.x] = gauss_box(cur.r[threadIdx.x].A, cur.r[threadIdx.x].B, &e);
             cur.ell[threadIdx.x] = e;
         }
         __syncthreads();
@@ -512,7 +669,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
                 mask &= mask - 1;
                 // The forward's decisions as predicates (every lane evaluates the candidate;
                 // a lane that does not blend it contributes zeros and keeps its state).
-                const float4 A = cur.A[j], B = cur.B[j];
+                const float4 A = cur.r[j].A, B = cur.r[j].B;
                 const float dx = A.x - pxf, dy = A.y - pyf;
                 const float power = gs_power(B.x, B.y, B.z, dx, dy);
                 const float G = gs_expf(power);
@@ -581,7 +738,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
             // moments (sum dpow dx, dpow dy, dpow dx^2, dpow dx dy, dpow dy^2) to the
             // gradients of the 2D mean and the conic
             {
-                const float4 B = cur.B[threadIdx.x];
+                const float4 B = cur.r[threadIdx.x].B;
                 float *a = acc[threadIdx.x];
                 const float mx = a[0], my = a[1], mxx = a[2], mxy = a[3], myy = a[4];
                 a[0] = -(B.x * mx + B.y * my);
@@ -603,7 +760,8 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p)
         }
         __syncthreads();
     }
-    cp_async_wait<0>();
+    if (TMA) tma_drain(mbar, phase, issued, waited, p.ws.spin_limit, p.ws.status);
+    else cp_async_wait<0>();
 }
 
 }  // namespace
@@ -628,6 +786,43 @@ static BlendParams make_params(const gsevt_frame *f, const Workspace &ws, const 
     return p;
 }
 
+// The record tensor of a frame for the TMA staging path: num_vg rows of 8 floats (32 bytes),
+// boxes of one row (what tile::gather4 copies four of).  false when the driver entry point or
+// the encoding is unavailable, in which case the blends stage with cp.async.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static bool record_tensor_map(const gsevt_frame *f, const Workspace &ws, CUtensorMap *tm)
+{
+    static std::atomic<EncodeTiledFn> encode{nullptr};
+    static std::atomic<int> resolved{0};
+    if (!resolved.load()) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            encode.store((EncodeTiledFn)fn);
+        resolved.store(1);
+    }
+    EncodeTiledFn enc = encode.load();
+    if (!enc || f->L.num_vg <= 0) return false;
+    const cuuint64_t dims[2] = {8, (cuuint64_t)f->L.num_vg};
+    const cuuint64_t strides[1] = {32};  // bytes between rows
+    const cuuint32_t box[2] = {8, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)ws.rec, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// TMA staging is used for the grey tracker blends when the frame's tuning asks for it.
+static bool use_tma(const gsevt_frame *f, const Workspace &ws, CUtensorMap *tm)
+{
+    std::memset(tm, 0, sizeof(*tm));
+    return f->L.tuning.blend_staging == 2 && f->L.channels == 1 && record_tensor_map(f, ws, tm);
+}
+
 int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s)
 {
     if (f->L.total_tiles <= 0) return GSEVT_OK;
@@ -635,12 +830,15 @@ int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     if (f->n_touched) cudaMemsetAsync(f->n_touched, 0, (size_t)f->L.num_vg * 4, s);
     const int n = f->L.total_tiles;
     const bool extras = f->depth || f->alpha || f->n_contrib || f->n_touched;
+    CUtensorMap tm;
+    const bool tma = !extras && use_tma(f, ws, &tm);
     if (p.rgb) {
-        if (extras) k_blend_fwd<true, true><<<n, GS_BLOCK, 0, s>>>(p);
-        else k_blend_fwd<false, true><<<n, GS_BLOCK, 0, s>>>(p);
+        if (extras) k_blend_fwd<true, true, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+        else k_blend_fwd<false, true, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
     } else {
-        if (extras) k_blend_fwd<true, false><<<n, GS_BLOCK, 0, s>>>(p);
-        else k_blend_fwd<false, false><<<n, GS_BLOCK, 0, s>>>(p);
+        if (extras) k_blend_fwd<true, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+        else if (tma) k_blend_fwd<false, false, true><<<n, GS_BLOCK, 0, s>>>(p, tm);
+        else k_blend_fwd<false, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
     }
     GS_CUDA_CHECK();
     return GSEVT_OK;
@@ -654,9 +852,12 @@ int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     p.dL_dimage = dL_dimage;
     p.dL_ddepth = dL_ddepth;
     p.dL_dalpha = dL_dalpha;
-    if (p.rgb) k_blend_bwd<2><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
-    else if (dL_dimage) k_blend_bwd<1><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
-    else k_blend_bwd<0><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p);
+    CUtensorMap tm;
+    const bool tma = !p.rgb && !dL_dimage && use_tma(f, ws, &tm);
+    if (p.rgb) k_blend_bwd<2, false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p, tm);
+    else if (dL_dimage) k_blend_bwd<1, false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p, tm);
+    else if (tma) k_blend_bwd<0, true><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p, tm);
+    else k_blend_bwd<0, false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p, tm);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

@@ -89,7 +89,8 @@ extern "C" void gsevt_workspace_offsets(const gsevt_layout *L, uint64_t *out)
     // carve against a fake non-null base so absent regions stay null
     char *base = (char *)(uintptr_t)4096;
     Workspace w = gs_carve(*L, base);
-    const void *ptrs[GS_WS_REGIONS] = {w.status, w.bin, w.recA, w.recB, w.recC, w.gradA, w.gradB, w.gradC,
+    // recA / recB: the two halves of the interleaved 32-byte blend records
+    const void *ptrs[GS_WS_REGIONS] = {w.status, w.bin, w.rec, w.rec + 1, w.recC, w.gradA, w.gradB, w.gradC,
                                        w.vis_sums, w.vis_offs, w.dkeys[0], w.dkeys[1], w.dvals[0], w.dvals[1],
                                        w.tsums, w.toffs, w.keys[0], w.keys[1], w.vals[0], w.vals[1], w.sort_hist,
                                        w.sort_counter, w.sort_lookback, w.ranges, w.loss_part, w.loss_scal,

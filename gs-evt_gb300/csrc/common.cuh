@@ -85,8 +85,8 @@ struct Workspace {
                           // [5] number of visible (view, Gaussian) slots, [6] number of coarse
                           // (super-tile, slot) pairs, [7] fine-list region cursor
     int4 *bin;            // [num_vg] {touched, rect lo (x0 | y0<<16), rect hi, depth bits}
-    float4 *recA;         // [num_vg] {mean x, mean y, depth, grey}
-    float4 *recB;         // [num_vg] {conic x, y, z, opacity}
+    float4 *rec;          // [num_vg][2] the blend record of each slot, 32 bytes:
+                          // {mean x, mean y, depth, grey}, {conic x, y, z, opacity}
     float4 *recC;         // [num_vg] {r, g, b, 0} (channels == 3)
     float4 *gradA;        // [num_vg] dL/d{mean x, mean y, conic x, conic y}
     float4 *gradB;        // [num_vg] dL/d{conic z, opacity, grey or r, depth}
@@ -117,7 +117,13 @@ struct Workspace {
                           // twist-only adjoint (frames with render pairs; else absent)
     size_t bytes;
     uint32_t spin_limit;  // polls of a bounded wait before it gives up (the layout's, or GS_SPIN_LIMIT)
+    int depth_kpt;        // keys per thread of the onesweep depth sort (4, 8 or 12)
+    int pair_kpt;         // keys per thread of the onesweep pair sorts (4, 8 or 12)
+    int coop_ok;          // the cooperative sort may be used
 };
+
+// keys per thread of a tuning field: 4, 8 or 12 (anything else: the default)
+inline int gs_kpt_choice(int32_t v, int dflt) { return (v == 4 || v == 8 || v == 12) ? (int)v : dflt; }
 
 #define GS_WS_REGIONS 34
 #define GS_FCACHE 6       // float4 words per slot in fcache
@@ -127,11 +133,13 @@ __host__ __device__ inline size_t gs_align(size_t x) { return (x + 255) & ~(size
 
 inline uint32_t gs_sort_tiles(uint32_t cap, int kpt) { return (cap + GS_BLOCK * kpt - 1) / (GS_BLOCK * kpt); }
 inline uint32_t gs_sorted_blocks(const gsevt_layout &L) { return ((uint32_t)(L.num_vg > 0 ? L.num_vg : 1) + GS_BLOCK - 1) / GS_BLOCK; }
+// look-back entries of the onesweep sorts: enough for the smallest keys-per-thread choice (4),
+// so that a tuning change never needs a larger workspace
 inline uint32_t gs_lookback_tiles(const gsevt_layout &L)
 {
     uint32_t cap = L.key_capacity > 0 ? L.key_capacity : 1;
     uint32_t vg = L.num_vg > 0 ? (uint32_t)L.num_vg : 1;
-    return std::max(gs_sort_tiles(cap, GS_SORT_KPT_TILES), gs_sort_tiles(vg, GS_SORT_KPT_DEPTH));
+    return std::max(gs_sort_tiles(cap, 4), gs_sort_tiles(vg, 4));
 }
 inline int gs_tile_bits(const gsevt_layout &L) { return L.sort_bits - 32; }
 // number of super-tile ids: the layout's exact count, else an upper bound
@@ -173,8 +181,7 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     bool rgb = L.channels == 3;
     w.status = (uint32_t *)take(64);
     w.bin = (int4 *)take(vg * 16);
-    w.recA = (float4 *)take(vg * 16);
-    w.recB = (float4 *)take(vg * 16);
+    w.rec = (float4 *)take(vg * 32);
     w.recC = rgb ? (float4 *)take(vg * 16) : nullptr;
     w.gradA = (float4 *)take(vg * 16);
     w.gradB = (float4 *)take(vg * 16);
@@ -208,6 +215,9 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     w.fcache = (L.num_pairs > 0 && !rgb) ? (float4 *)take(vg * GS_FCACHE * 16) : nullptr;
     w.bytes = off;
     w.spin_limit = L.spin_limit ? L.spin_limit : GS_SPIN_LIMIT;
+    w.depth_kpt = gs_kpt_choice(L.tuning.depth_sort_kpt, GS_SORT_KPT_DEPTH);
+    w.pair_kpt = gs_kpt_choice(L.tuning.pair_sort_kpt, GS_SORT_KPT_TILES);
+    w.coop_ok = L.tuning.coop_sort != 1;
     return w;
 }
 

@@ -349,8 +349,8 @@ __global__ void __launch_bounds__(GS_BLOCK, 2) k_preprocess_fwd(FwdParams p)
                 float grey = grey_of(o.rgb);
                 p.ws.bin[vg] = make_int4((int)touched, o.rect[0] | (o.rect[1] << 16),
                                          o.rect[2] | (o.rect[3] << 16), __float_as_int(o.pc[2]));
-                p.ws.recA[vg] = make_float4(o.mean[0], o.mean[1], o.pc[2], grey);
-                p.ws.recB[vg] = make_float4(o.conic[0], o.conic[1], o.conic[2], a.opac);
+                p.ws.rec[2 * vg] = make_float4(o.mean[0], o.mean[1], o.pc[2], grey);
+                p.ws.rec[2 * vg + 1] = make_float4(o.conic[0], o.conic[1], o.conic[2], a.opac);
                 if (p.rgb) p.ws.recC[vg] = make_float4(o.rgb[0], o.rgb[1], o.rgb[2], 0.0f);
                 if (p.ws.fcache) write_fcache(p.ws.fcache + vg * GS_FCACHE, o, a.cov, a.sh, M.sh_degree, a.has_col);
             } else {

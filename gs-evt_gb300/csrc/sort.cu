@@ -884,7 +884,7 @@ bool launch_coop(uint32_t *const keys[2], uint32_t *const vals[2], const uint32_
                  const GsCompact *cmp = nullptr)
 {
     const int g = coop_grid_here();
-    if (g <= 0 || (uint64_t)capacity > (uint64_t)g * GS_COOP_TILE) return false;
+    if (!ws.coop_ok || g <= 0 || (uint64_t)capacity > (uint64_t)g * GS_COOP_TILE) return false;
     if (cmp && (uint64_t)cmp->num_scan_blocks * GS_BLOCK > (uint64_t)g * GS_COOP_TILE) return false;
     cudaMemsetAsync(ws.sort_counter, 0, 4, s);
     CoopParams cp;
@@ -954,7 +954,7 @@ int gs_launch_depth_sort(const Workspace &ws, uint32_t capacity, const GsCompact
     }
     if (cmp) return GSEVT_ERR_ARG;  // the compaction runs only inside the cooperative sort
     int buf = 0;
-    st = gs_launch_sort_t<uint32_t>(dk, dv, ws.status + 5, capacity, 32, capacity, GS_SORT_KPT_DEPTH, ws, &buf, s,
+    st = gs_launch_sort_t<uint32_t>(dk, dv, ws.status + 5, capacity, 32, capacity, ws.depth_kpt, ws, &buf, s,
                                     nullptr, 0);
     if (st) return st;
     return buf == 0 ? GSEVT_OK : GSEVT_ERR_ARG;  // 4 passes: the result is back in buffer 0

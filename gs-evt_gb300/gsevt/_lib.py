@@ -24,9 +24,11 @@ STATUS_KEY_OVERFLOW = 1
 STATUS_SORT_TIMEOUT = 2
 STATUS_NONFINITE = 4
 STATUS_LAYOUT = 8
+STATUS_STAGE_TIMEOUT = 16
 _STATUS_NAMES = ((STATUS_KEY_OVERFLOW, "key capacity overflow"), (STATUS_SORT_TIMEOUT, "bounded device wait ran out"),
                  (STATUS_NONFINITE, "non-finite loss or gradient"),
-                 (STATUS_LAYOUT, "layout provides too few super-tiles"))
+                 (STATUS_LAYOUT, "layout provides too few super-tiles"),
+                 (STATUS_STAGE_TIMEOUT, "blend staging wait ran out"))
 
 
 def status_names(flags):
@@ -78,13 +80,18 @@ class Pair(C.Structure):
                 ("log_eps", C.c_float)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("blend_staging", C.c_int32), ("depth_sort_kpt", C.c_int32), ("pair_sort_kpt", C.c_int32),
+                ("coop_sort", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+
 class Layout(C.Structure):
     _fields_ = [("num_views", C.c_int32), ("num_maps", C.c_int32), ("num_pairs", C.c_int32),
                 ("num_vg", C.c_int32), ("num_scan_blocks", C.c_int32),
                 ("preprocess_blocks", C.c_int32), ("total_tiles", C.c_int32),
                 ("total_pixels", C.c_int32), ("channels", C.c_int32), ("sort_bits", C.c_int32),
                 ("key_capacity", C.c_uint32), ("loss_blocks", C.c_int32), ("super_tiles", C.c_int32),
-                ("spin_limit", C.c_uint32)]
+                ("spin_limit", C.c_uint32), ("tuning", Tuning)]
 
 
 class Frame(C.Structure):

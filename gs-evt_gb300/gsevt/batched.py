@@ -44,9 +44,11 @@ def _field(name):
 
 
 class BatchedTracker:
-    def __init__(self, maps, problems, key_capacity=None, device="cuda", key_margin=1.3):
+    def __init__(self, maps, problems, key_capacity=None, device="cuda", key_margin=1.3, tuning="table"):
         """maps: list of dicts with xyz, opacity, sh, scale, rot (numpy or tensors) or
-        already-packed tensors under "packed" with "n"."""
+        already-packed tensors under "packed" with "n".  tuning: "table" (the autotuner's
+        choice for this workload shape when its table has one, else the defaults),
+        "defaults", or a dict of gsevt_tuning fields."""
         self.device = torch.device(device)
         order = sorted(range(len(problems)), key=lambda i: problems[i].map_index)
         self.problems = [problems[i] for i in order]
@@ -83,6 +85,16 @@ class BatchedTracker:
         self.graph = None
         if key_capacity is None:
             self.fit_capacity(key_margin)
+        self.tuning_source = "defaults"
+        if isinstance(tuning, dict):
+            self.frame.set_tuning(**tuning)
+            self.tuning_source = "given"
+        elif tuning == "table":
+            from . import tuner
+            choice = tuner.lookup(self.frame.L)
+            if choice:
+                self.frame.set_tuning(**choice)
+                self.tuning_source = "table"
 
     # ---------------------------------------------------------------- state --
     def _init_states(self):

@@ -259,6 +259,18 @@ class GSFrame:
         raw = torch.frombuffer(bytearray(bytes(s)), dtype=torch.uint8)
         self.view_table[i * C.sizeof(_lib.View):(i + 1) * C.sizeof(_lib.View)].copy_(raw)
 
+    def set_tuning(self, **choices):
+        """Launch choices (gsevt_tuning fields: blend_staging, depth_sort_kpt, pair_sort_kpt,
+        coop_sort); unnamed fields keep their values.  A CUDA graph captured before keeps
+        the launches it recorded."""
+        for k, v in choices.items():
+            setattr(self.L.tuning, k, int(v))
+            setattr(self._frame.L.tuning, k, int(v))
+
+    def tuning(self):
+        t = self.L.tuning
+        return {k: int(getattr(t, k)) for k in ("blend_staging", "depth_sort_kpt", "pair_sort_kpt", "coop_sort")}
+
     def set_spin_limit(self, limit):
         """Polls a bounded device wait makes before it gives up (0: the library default)."""
         self.L.spin_limit = int(limit)

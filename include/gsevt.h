@@ -53,6 +53,7 @@ enum {
 #define GSEVT_STATUS_SORT_TIMEOUT 2u
 #define GSEVT_STATUS_NONFINITE 4u
 #define GSEVT_STATUS_LAYOUT 8u /* the views need more super-tiles than layout.super_tiles */
+#define GSEVT_STATUS_STAGE_TIMEOUT 16u /* a blend's wait for its staged batch ran out */
 
 #define GSEVT_TILE 16
 #define GSEVT_LOSS_PIXELS_PER_BLOCK 2048 /* pixels reduced by one loss block */
@@ -135,6 +136,19 @@ typedef struct gsevt_pair {
     float log_eps;           /* offset inside the logarithm (log_grey only), > 0 */
 } gsevt_pair;
 
+/* Launch choices of a frame; all zeros select the library's defaults.  The autotuner
+ * (gsevt.tuner) times the alternatives per workload shape and keeps the fastest. */
+typedef struct gsevt_tuning {
+    int32_t blend_staging;   /* how a blend block stages its batch of 256 records in shared
+                              * memory: 0 or 1, one 16-byte cp.async per record half and thread;
+                              * 2, TMA tile::gather4 tensor copies issued by one warp (the grey
+                              * tracker blends; the RGB drop-in blends always use cp.async) */
+    int32_t depth_sort_kpt;  /* keys per thread of the onesweep depth sort: 0 (= 12), 4, 8, 12 */
+    int32_t pair_sort_kpt;   /* keys per thread of the onesweep pair sorts: 0 (= 12), 4, 8, 12 */
+    int32_t coop_sort;       /* 0: sorts that fit run as one cooperative launch, 1: never */
+    int32_t reserved[4];
+} gsevt_tuning;
+
 /* Sizes of one rendering frame (host struct). */
 typedef struct gsevt_layout {
     int32_t num_views, num_maps, num_pairs;
@@ -157,6 +171,7 @@ typedef struct gsevt_layout {
                                  * image, loss or pose update) until the status is cleared,
                                  * which every gsevt_preprocess_fwd and
                                  * gsevt_track_step_batched call does first. */
+    gsevt_tuning tuning;        /* launch choices (zeros: defaults) */
 } gsevt_layout;
 
 /* One rendering frame: layout, device tables, workspace and caller-owned outputs. */
@@ -186,7 +201,8 @@ int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream);
  * frame, pose_state (7 entries).  Touches no GPU state. */
 void gsevt_abi_sizes(int32_t *out7);
 /* Byte offsets of the workspace regions for a layout (introspection for tests and
- * tools), in this order: status, bin, recA, recB, recC, gradA, gradB, gradC, vis_sums,
+ * tools), in this order: status, bin, recA, recB (the two float4 halves of one 32-byte
+ * record per slot, so both have a 32-byte stride), recC, gradA, gradB, gradC, vis_sums,
  * vis_offs, dkeys0, dkeys1, dvals0, dvals1, tsums, toffs, keys0, keys1, vals0, vals1,
  * sort_hist, sort_counter, sort_lookback, ranges, loss_part, loss_scal, loss_done,
  * xi_part, xi, csums, coffs, soffs, sranges, fcache (34 entries; absent regions are

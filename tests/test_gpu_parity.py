@@ -85,8 +85,8 @@ def test_single_view_bit_exact(small, packed):
     assert np.array_equal(binv[:, 0], pre["touched"])
     rect = pre["rect"][vis]
     assert np.array_equal(binv[vis, 1] & 0xffff, rect[:, 0]) and np.array_equal(binv[vis, 2] >> 16, rect[:, 3])
-    A = _region(fr, "recA", torch.float32, 4 * n).view(n, 4).cpu().numpy()[vis]
-    B = _region(fr, "recB", torch.float32, 4 * n).view(n, 4).cpu().numpy()[vis]
+    rec = _region(fr, "recA", torch.float32, 8 * n).view(n, 8).cpu().numpy()  # 32-byte records
+    A, B = rec[vis, :4], rec[vis, 4:]
     Cc = _region(fr, "recC", torch.float32, 4 * n).view(n, 4).cpu().numpy()[vis]
     assert _bits_equal(A[:, :2], pre["mean2d"][vis]) and _bits_equal(A[:, 2], pre["depth"][vis])
     assert _bits_equal(A[:, 3], pre["grey"][vis])
@@ -397,3 +397,49 @@ def test_batched_iteration_matches_plain_path(log_eps):
     np.testing.assert_allclose(st["t"][0], c.T.cpu().numpy(), atol=2e-6)
     np.testing.assert_allclose(st["ang_vel"][0], c.angular_vel.cpu().numpy(), atol=2e-6)
     np.testing.assert_allclose(st["lin_vel"][0], c.linear_vel.cpu().numpy(), atol=2e-6)
+
+
+@pytest.mark.parametrize("depth_kpt,pair_kpt,coop_sort", [(4, 4, 0), (8, 8, 1), (12, 4, 1)])
+def test_sort_tuning_choices_keep_order_bit_exact(small, depth_kpt, pair_kpt, coop_sort):
+    """Every sort configuration the autotuner may pick (onesweep keys per thread 4 / 8 / 12,
+    the cooperative sort allowed or not) gives the oracle's keys, sort order, ranges and
+    image bit for bit.  A 2M key capacity makes the tile sort run the onesweep passes."""
+    m, cam, R, t = small
+    W, H = cam.width, cam.height
+    s, _ = _map_spec(m, True)
+    fr = GSFrame([s], [_view(R, t, cam)], channels=1, key_capacity=2_000_000, device=DEV)
+    fr.set_tuning(depth_sort_kpt=depth_kpt, pair_sort_kpt=pair_kpt, coop_sort=coop_sort)
+    fr.render(exact_keys=True)
+    torch.cuda.synchronize()
+    assert fr.status()[0] == 0
+    res = oracle.rasterize_view(m["xyz"], helpers.cov6(m), m["sh"], m["opacity"], helpers.view_vector(R, t, cam),
+                                W, H, [0.0], nch=1)
+    K = fr.num_keys
+    buf = ((fr.L.sort_bits - 32 + 7) // 8) & 1
+    vals = _region(fr, "vals%d" % buf, torch.int32, K).cpu().numpy().view(np.uint32)
+    assert np.array_equal(vals, res["vals"])
+    rng = _region(fr, "ranges", torch.int32, 2 * fr.L.total_tiles).view(-1, 2).cpu().numpy().view(np.uint32)
+    assert np.array_equal(rng, res["ranges"])
+    assert _bits_equal(fr.pixels(0)[0].cpu().numpy(), res["image"][0])
+
+
+def test_batched_step_without_the_cooperative_sort_matches():
+    """The batched step with the cooperative sort turned off (visible-slot compaction,
+    onesweep depth sort, coarse duplication and the super-tile sort as separate kernels, the
+    path of frames above 8192 slots per SM) renders the same images, loss and gradient."""
+    from gsevt.batched import BatchedTracker, Problem
+    m, cam, R, t, lin, ang, dtau, E = _pair_setup(n=20000, W=320, H=240, f=300.0, seed=0, pose_seed=33)
+    out = []
+    for coop in (0, 1):
+        prob = Problem(0, R, t, lin, ang, dtau, cam.width, cam.height, cam.fx, cam.fy, _t(E.reshape(-1)),
+                       lr=(0.0, 0.0, 0.0, 0.0), opt_vel=True)
+        bt = BatchedTracker([m], [prob], device=DEV)
+        bt.frame.set_tuning(coop_sort=coop, depth_sort_kpt=8)
+        bt.step()
+        torch.cuda.synchronize()
+        assert bt.check_status()[0] == 0
+        out.append((bt.frame.image.clone(), bt.states()))
+    (i0, s0), (i1, s1) = out
+    assert torch.equal(i0.view(torch.int32), i1.view(torch.int32))
+    assert s0["loss"][0] == s1["loss"][0]
+    assert np.linalg.norm(s0["grad"][0] - s1["grad"][0]) <= 1e-5 * np.linalg.norm(s0["grad"][0])

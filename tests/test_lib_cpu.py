@@ -44,7 +44,9 @@ def test_workspace_sizing_and_offsets():
     assert big >= small + 100000 * 16  # two key and two value buffers of 4 bytes
     off = _lib.workspace_offsets(L)
     assert off["status"] == 0 and off["recC"] is None and off["gradC"] is None
-    seen = [v for v in off.values() if v is not None]
+    # recA / recB are the two 16-byte halves of one 32-byte record per slot
+    assert off["recB"] == off["recA"] + 16
+    seen = [v for k, v in off.items() if v is not None and k != "recB"]
     assert seen == sorted(seen) and all(v % 256 == 0 for v in seen)
     # the sort-count region also holds the cooperative sort's digit-major table:
     # 256 digits x 160 block columns plus 256 row totals, 32-bit each
@@ -75,3 +77,25 @@ def test_status_names():
         "key capacity overflow, layout provides too few super-tiles")
     assert _lib.status_names(_lib.STATUS_SORT_TIMEOUT) == "bounded device wait ran out"
     assert "unknown flags 0x40" in _lib.status_names(0x40 | _lib.STATUS_NONFINITE)
+
+
+def test_tuning_table_round_trip(tmp_path):
+    """The autotuner's table: shape keys, record / save / load / lookup, and the layout's
+    tuning struct in the binding."""
+    from gsevt import tuner
+    L = _lib.Layout()
+    L.num_views, L.num_maps, L.num_vg, L.total_pixels = 2, 1, 1_000_000, 614400
+    key = tuner.shape_key(L)
+    assert key == "v2-m1-g1000000-p614400"
+    trials = [(dict(tuner.DEFAULTS), 0.64), (dict(tuner.DEFAULTS, blend_staging=2), 0.62)]
+    path = str(tmp_path / "table.json")
+    table = tuner.record({}, L, trials[1][0], 0.62, trials, workload="w", device="d")
+    tuner.save_table(table, path)
+    loaded = tuner.load_table(path)
+    assert loaded[key]["default_ms"] == 0.64
+    assert tuner.lookup(L, loaded) == dict(tuner.DEFAULTS, blend_staging=2)
+    L.num_vg += 1
+    assert tuner.lookup(L, loaded) is None
+    assert tuner.load_table(str(tmp_path / "missing.json")) == {}
+    L.tuning.blend_staging = 2
+    assert bytes(L)[-32:-28] == (2).to_bytes(4, "little")  # the struct's first tuning field
