@@ -59,6 +59,10 @@ struct BlendParams {
     float *image, *final_T, *depth, *alpha;
     int32_t *n_contrib, *n_touched;
     const float *dL_dimage, *dL_ddepth, *dL_dalpha;
+    // persistent launches: the tiles in the order blocks take them, and the queue head
+    const uint32_t *order;
+    uint32_t *queue;
+    int num_tiles;
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -240,13 +244,14 @@ __device__ __forceinline__ void tma_load_batch(const BlendParams &p, Batch<RGB> 
 // Before a block exits: wait (bounded) for the batch it issued but did not consume (at
 // most one, batch `waited`, when the block stopped early), so that no tensor copy still
 // targets its shared memory.
-__device__ __forceinline__ void tma_drain(uint64_t *mbar, uint32_t phase, int issued, int waited, uint32_t limit,
+__device__ __forceinline__ void tma_drain(uint64_t *mbar, uint32_t &phase, int issued, int waited, uint32_t limit,
                                           uint32_t *status)
 {
     if (issued > waited) {
         const int b = waited & 1;
         if (!mbar_wait(&mbar[b], (phase >> b) & 1u, limit) && threadIdx.x == 0)
             atomicOr(status, GSEVT_STATUS_STAGE_TIMEOUT);
+        phase ^= 1u << b;
     }
 }
 
@@ -303,23 +308,12 @@ __device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const Blend
 // EXTRAS: the frame wants depth, alpha, contributor counts or n_touched (each still
 // checked at run time); without it only the image and the final transmittance are
 // accumulated (the batched tracker's case).
+// Blends one tile (all threads of the block).  V is the tile's view; with TMA, `phase`
+// carries the buffers' mbarrier parities from tile to tile.
 template <bool EXTRAS, bool RGB, bool TMA>
-__global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams p, const __grid_constant__ CUtensorMap tm)
+__device__ __forceinline__ void fwd_tile(const BlendParams &p, const CUtensorMap *tm, int tile, Batch<RGB> (&sb)[2],
+                                         const gsevt_view &V, uint64_t *mbar, uint32_t &phase)
 {
-    __shared__ Batch<RGB> sb[2];
-    __shared__ gsevt_view V;
-    __shared__ __align__(8) uint64_t mbar[2];
-    const int tile = blockIdx.x;
-    if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
-    if (threadIdx.x == 0) {
-        V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
-        if (TMA) {
-            mbar_init(&mbar[0]);
-            mbar_init(&mbar[1]);
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-    }
-    __syncthreads();
     const int lt = tile - V.tile_offset;
     const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
     int px, py;
@@ -334,11 +328,10 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
     int last = 0;
     bool done = !inside;
     const int lane = threadIdx.x & 31;
-    uint32_t phase = 0;  // TMA: parity of the next phase of each buffer's mbarrier (bit b)
     int issued = 0, waited = 0;  // TMA: batches issued / waited for
     if (rounds > 0) {
         if (TMA) {
-            if (threadIdx.x < 32) tma_load_batch(p, sb[0], range, 0, &mbar[0], &tm);
+            if (threadIdx.x < 32) tma_load_batch(p, sb[0], range, 0, &mbar[0], tm);
             issued = 1;
         } else {
             load_batch(p, sb[0], range, 0);
@@ -348,7 +341,7 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
         Batch<RGB> &cur = sb[r & 1];
         if (TMA) {
             if (r + 1 < rounds) {
-                if (threadIdx.x < 32) tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], &tm);
+                if (threadIdx.x < 32) tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], tm);
                 issued = r + 2;
             }
             if (!mbar_wait(&mbar[r & 1], (phase >> (r & 1)) & 1u, p.ws.spin_limit) && threadIdx.x == 0)
@@ -410,6 +403,45 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
             if (p.alpha) p.alpha[pix] = Aacc;
             if (p.n_contrib) p.n_contrib[pix] = last;
         }
+    }
+}
+
+// The next tile of a block, in thread 0: its own tile (one block per tile), or with
+// PERSIST the next entry of the tile order (blocks stay resident and take tiles from one
+// queue, longest lists first); -1 when there is none.
+template <bool PERSIST>
+__device__ __forceinline__ int next_tile(const BlendParams &p, int it)
+{
+    if (!PERSIST) return it == 0 ? (int)blockIdx.x : -1;
+    const uint32_t q = atomicAdd(p.queue, 1u);
+    return q < (uint32_t)p.num_tiles ? (int)p.order[q] : -1;
+}
+
+template <bool EXTRAS, bool RGB, bool TMA, bool PERSIST>
+__global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams p, const __grid_constant__ CUtensorMap tm)
+{
+    __shared__ Batch<RGB> sb[2];
+    __shared__ gsevt_view V;
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int s_tile;
+    if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
+    if (TMA && threadIdx.x == 0) {
+        mbar_init(&mbar[0]);
+        mbar_init(&mbar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    uint32_t phase = 0;  // TMA: parity of the next phase of each buffer's mbarrier (bit b)
+    for (int it = 0;; ++it) {
+        if (threadIdx.x == 0) {
+            const int t = next_tile<PERSIST>(p, it);
+            s_tile = t;
+            if (t >= 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, t)];
+        }
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile < 0) break;
+        fwd_tile<EXTRAS, RGB, TMA>(p, &tm, tile, sb, V, mbar, phase);
+        __syncthreads();  // V, s_tile and the batch buffers are reused by the next tile
     }
 }
 
@@ -524,27 +556,14 @@ __device__ __forceinline__ float warp_reduce_pair6(const float (&a)[6], const fl
     return v[0];
 }
 
+// The adjoint of one tile (all threads of the block); acc is zero on entry and on exit.
 template <int MODE, bool TMA>
-__global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p, const __grid_constant__ CUtensorMap tm)
+__device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap *tm, int tile,
+                                         Batch<MODE == 2> (&sb)[2], float (*acc)[Comps<MODE>::n + 1],
+                                         const gsevt_view &V, uint64_t *mbar, uint32_t &phase)
 {
     constexpr bool RGB = MODE == 2;
     constexpr int NC = Comps<MODE>::n;
-    __shared__ Batch<RGB> sb[2];
-    __shared__ float acc[GS_BLOCK][NC + 1];
-    __shared__ gsevt_view V;
-    __shared__ __align__(8) uint64_t mbar[2];
-    const int tile = blockIdx.x;
-    if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
-    if (threadIdx.x == 0) {
-        V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
-        if (TMA) {
-            mbar_init(&mbar[0]);
-            mbar_init(&mbar[1]);
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-    }
-    for (int i = threadIdx.x; i < GS_BLOCK * (NC + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int lt = tile - V.tile_offset;
     const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
@@ -601,11 +620,10 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p, const __g
 
     float T = 1.0f, Pc[3] = {0, 0, 0}, PD = 0.0f, PA = 0.0f;
     bool done = !inside;
-    uint32_t phase = 0;  // TMA: parity of the next phase of each buffer's mbarrier (bit b)
     int issued = 0, waited = 0;  // TMA: batches issued / waited for
     if (rounds > 0) {
         if (TMA) {
-            if (threadIdx.x < 32) tma_load_batch(p, sb[0], range, 0, &mbar[0], &tm);
+            if (threadIdx.x < 32) tma_load_batch(p, sb[0], range, 0, &mbar[0], tm);
             issued = 1;
         } else {
             load_batch(p, sb[0], range, 0);
@@ -615,7 +633,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p, const __g
         Batch<RGB> &cur = sb[r & 1];
         if (TMA) {
             if (r + 1 < rounds) {
-                if (threadIdx.x < 32) tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], &tm);
+                if (threadIdx.x < 32) tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], tm);
                 issued = r + 2;
             }
             if (!mbar_wait(&mbar[r & 1], (phase >> (r & 1)) & 1u, p.ws.spin_limit) && threadIdx.x == 0)
@@ -764,6 +782,70 @@ __global__ void __launch_bounds__(GS_BLOCK) k_blend_bwd(BlendParams p, const __g
     else cp_async_wait<0>();
 }
 
+// the tracker adjoint (MODE 0) keeps five blocks per SM (its shared memory allows five)
+template <int MODE, bool TMA, bool PERSIST>
+__global__ void __launch_bounds__(GS_BLOCK, MODE == 0 ? 5 : 1) k_blend_bwd(BlendParams p,
+                                                                         const __grid_constant__ CUtensorMap tm)
+{
+    constexpr bool RGB = MODE == 2;
+    constexpr int NC = Comps<MODE>::n;
+    __shared__ Batch<RGB> sb[2];
+    __shared__ float acc[GS_BLOCK][NC + 1];
+    __shared__ gsevt_view V;
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int s_tile;
+    if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
+    if (TMA && threadIdx.x == 0) {
+        mbar_init(&mbar[0]);
+        mbar_init(&mbar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int i = threadIdx.x; i < GS_BLOCK * (NC + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
+    uint32_t phase = 0;  // TMA: parity of the next phase of each buffer's mbarrier (bit b)
+    for (int it = 0;; ++it) {
+        if (threadIdx.x == 0) {
+            const int t = next_tile<PERSIST>(p, it);
+            s_tile = t;
+            if (t >= 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, t)];
+        }
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile < 0) break;
+        bwd_tile<MODE, TMA>(p, &tm, tile, sb, acc, V, mbar, phase);
+        __syncthreads();  // V, s_tile and the batch buffers are reused by the next tile
+    }
+}
+
+// Orders the tiles for the persistent blends: descending list length in 33 buckets
+// (bucket 1 + floor(log2 len), empty lists last), so that the blocks that finish last take
+// short tiles.  One block; also clears the two queue heads (forward, adjoint).
+__global__ void __launch_bounds__(1024) k_tile_order(const uint2 *ranges, int num_tiles, uint32_t *order,
+                                                     uint32_t *queues)
+{
+    __shared__ uint32_t cnt[33], start[33];
+    const int t = threadIdx.x;
+    if (t < 33) cnt[t] = 0u;
+    __syncthreads();
+    for (int i = t; i < num_tiles; i += blockDim.x) {
+        const uint32_t len = ranges[i].y - ranges[i].x;
+        atomicAdd(&cnt[len ? 32 - __clz(len) : 0], 1u);
+    }
+    __syncthreads();
+    if (t == 0) {
+        uint32_t run = 0;
+        for (int b = 32; b >= 0; --b) {
+            start[b] = run;
+            run += cnt[b];
+        }
+        queues[0] = queues[1] = 0u;
+    }
+    __syncthreads();
+    for (int i = t; i < num_tiles; i += blockDim.x) {
+        const uint32_t len = ranges[i].y - ranges[i].x;
+        order[atomicAdd(&start[len ? 32 - __clz(len) : 0], 1u)] = (uint32_t)i;
+    }
+}
+
 }  // namespace
 
 static BlendParams make_params(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals)
@@ -783,7 +865,36 @@ static BlendParams make_params(const gsevt_frame *f, const Workspace &ws, const 
     p.n_contrib = f->n_contrib;
     p.n_touched = f->n_touched;
     p.dL_dimage = p.dL_ddepth = p.dL_dalpha = nullptr;
+    p.order = ws.keys[0];  // free once the tile lists are built (batched step)
+    p.queue = ws.status + 8;
+    p.num_tiles = f->L.total_tiles;
     return p;
+}
+
+// Persistent blends (gsevt_tuning.blend_schedule 1, batched step only): the tile order and
+// the queue heads live in the first pair-key buffer and status words 8-9.
+bool gs_blend_persistent(const gsevt_frame *f)
+{
+    return f->L.tuning.blend_schedule == 1 && f->L.channels == 1 && (uint32_t)f->L.total_tiles <= f->L.key_capacity;
+}
+
+int gs_launch_tile_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s)
+{
+    k_tile_order<<<1, 1024, 0, s>>>(ws.ranges, f->L.total_tiles, ws.keys[0], ws.status + 8);
+    GS_CUDA_CHECK();
+    return GSEVT_OK;
+}
+
+// resident blocks of a kernel on the current device (for the persistent grids)
+template <typename K>
+static int resident_grid(K kernel, int tiles)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                 cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, GS_BLOCK, 0) != cudaSuccess || per_sm < 1)
+        return tiles;
+    return std::min(tiles, sms * per_sm);
 }
 
 // The record tensor of a frame for the TMA staging path: num_vg rows of 8 floats (32 bytes),
@@ -823,7 +934,8 @@ static bool use_tma(const gsevt_frame *f, const Workspace &ws, CUtensorMap *tm)
     return f->L.tuning.blend_staging == 2 && f->L.channels == 1 && record_tensor_map(f, ws, tm);
 }
 
-int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s)
+int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s,
+                        bool persist)
 {
     if (f->L.total_tiles <= 0) return GSEVT_OK;
     BlendParams p = make_params(f, ws, vals);
@@ -833,19 +945,30 @@ int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     CUtensorMap tm;
     const bool tma = !extras && use_tma(f, ws, &tm);
     if (p.rgb) {
-        if (extras) k_blend_fwd<true, true, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
-        else k_blend_fwd<false, true, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+        if (extras) k_blend_fwd<true, true, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+        else k_blend_fwd<false, true, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+    } else if (extras) {
+        k_blend_fwd<true, false, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+    } else if (persist) {
+        p.queue = ws.status + 8;
+        if (tma) {
+            auto k = k_blend_fwd<false, false, true, true>;
+            k<<<resident_grid(k, n), GS_BLOCK, 0, s>>>(p, tm);
+        } else {
+            auto k = k_blend_fwd<false, false, false, true>;
+            k<<<resident_grid(k, n), GS_BLOCK, 0, s>>>(p, tm);
+        }
+    } else if (tma) {
+        k_blend_fwd<false, false, true, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
     } else {
-        if (extras) k_blend_fwd<true, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
-        else if (tma) k_blend_fwd<false, false, true><<<n, GS_BLOCK, 0, s>>>(p, tm);
-        else k_blend_fwd<false, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+        k_blend_fwd<false, false, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
     }
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }
 
 int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, const float *dL_dimage,
-                        const float *dL_ddepth, const float *dL_dalpha, cudaStream_t s)
+                        const float *dL_ddepth, const float *dL_dalpha, cudaStream_t s, bool persist)
 {
     if (f->L.total_tiles <= 0) return GSEVT_OK;
     BlendParams p = make_params(f, ws, vals);
@@ -854,10 +977,25 @@ int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     p.dL_dalpha = dL_dalpha;
     CUtensorMap tm;
     const bool tma = !p.rgb && !dL_dimage && use_tma(f, ws, &tm);
-    if (p.rgb) k_blend_bwd<2, false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p, tm);
-    else if (dL_dimage) k_blend_bwd<1, false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p, tm);
-    else if (tma) k_blend_bwd<0, true><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p, tm);
-    else k_blend_bwd<0, false><<<f->L.total_tiles, GS_BLOCK, 0, s>>>(p, tm);
+    const int n = f->L.total_tiles;
+    if (p.rgb) {
+        k_blend_bwd<2, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+    } else if (dL_dimage) {
+        k_blend_bwd<1, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+    } else if (persist) {
+        p.queue = ws.status + 9;
+        if (tma) {
+            auto k = k_blend_bwd<0, true, true>;
+            k<<<resident_grid(k, n), GS_BLOCK, 0, s>>>(p, tm);
+        } else {
+            auto k = k_blend_bwd<0, false, true>;
+            k<<<resident_grid(k, n), GS_BLOCK, 0, s>>>(p, tm);
+        }
+    } else if (tma) {
+        k_blend_bwd<0, true, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+    } else {
+        k_blend_bwd<0, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+    }
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

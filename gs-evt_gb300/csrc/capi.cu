@@ -14,9 +14,12 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
 int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, uint32_t **fine_vals,
                          cudaStream_t s, bool binned);
 int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, cudaStream_t s);
-int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s);
+int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s,
+                        bool persist = false);
 int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, const float *dL_dimage,
-                        const float *dL_ddepth, const float *dL_dalpha, cudaStream_t s);
+                        const float *dL_ddepth, const float *dL_dalpha, cudaStream_t s, bool persist = false);
+bool gs_blend_persistent(const gsevt_frame *f);
+int gs_launch_tile_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
 int gs_launch_loss(const gsevt_frame *f, const Workspace &ws, double *loss_out, cudaStream_t s);
 int gs_launch_track_finalize(const gsevt_frame *f, const Workspace &ws, gsevt_pose_state *poses, int num_poses,
                              const double *loss, cudaStream_t s);
@@ -217,9 +220,11 @@ extern "C" int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *
     if ((st = gs_launch_depth_order(f, ws, s, true, &binned))) return st;
     uint32_t *fine = nullptr;
     if ((st = gs_launch_bin_coarse(f, ws, f->L.key_capacity, &fine, s, binned))) return st;
-    if ((st = gs_launch_blend_fwd(f, ws, fine, s))) return st;
+    const bool persist = gs_blend_persistent(f);
+    if (persist && (st = gs_launch_tile_order(f, ws, s))) return st;
+    if ((st = gs_launch_blend_fwd(f, ws, fine, s, persist))) return st;
     if ((st = gs_launch_loss(f, ws, loss_out, s))) return st;
-    if ((st = gs_launch_blend_bwd(f, ws, fine, nullptr, nullptr, nullptr, s))) return st;
+    if ((st = gs_launch_blend_bwd(f, ws, fine, nullptr, nullptr, nullptr, s, persist))) return st;
     if ((st = gs_launch_preprocess_bwd_cached(f, ws, s))) return st;
     return gs_launch_track_finalize(f, ws, poses, num_poses, loss_out, s);
 }

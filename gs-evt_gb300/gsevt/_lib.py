@@ -82,7 +82,7 @@ class Pair(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("blend_staging", C.c_int32), ("depth_sort_kpt", C.c_int32), ("pair_sort_kpt", C.c_int32),
-                ("coop_sort", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("coop_sort", C.c_int32), ("blend_schedule", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class Layout(C.Structure):

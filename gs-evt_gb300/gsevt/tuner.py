@@ -11,8 +11,9 @@ defaults over
     depth_sort_kpt   4 | 8 | 12   keys per thread of the onesweep depth sort
     pair_sort_kpt    4 | 8 | 12   keys per thread of the onesweep (super-)tile sorts
     coop_sort        0 (one cooperative launch when the sort fits) | 1 (never)
+    blend_schedule   0 (one block per tile) | 1 (resident blocks, one longest-first tile queue)
 
-(10 timings per pass, two passes).  Choices that a frame cannot use (the cooperative sort
+(11 timings per pass, two passes).  Choices that a frame cannot use (the cooperative sort
 of a frame above 8192 slots per SM, the onesweep passes of a sort that runs cooperatively)
 time alike and the defaults are kept for them.
 
@@ -28,8 +29,9 @@ import statistics
 import torch
 
 TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_table.json")
-DEFAULTS = {"blend_staging": 1, "depth_sort_kpt": 12, "pair_sort_kpt": 12, "coop_sort": 0}
-SPACE = {"blend_staging": (1, 2), "depth_sort_kpt": (4, 8, 12), "pair_sort_kpt": (4, 8, 12), "coop_sort": (0, 1)}
+DEFAULTS = {"blend_staging": 1, "depth_sort_kpt": 12, "pair_sort_kpt": 12, "coop_sort": 0, "blend_schedule": 0}
+SPACE = {"blend_staging": (1, 2), "blend_schedule": (0, 1), "depth_sort_kpt": (4, 8, 12), "pair_sort_kpt": (4, 8, 12),
+         "coop_sort": (0, 1)}
 
 
 def shape_key(layout):

@@ -146,7 +146,10 @@ typedef struct gsevt_tuning {
     int32_t depth_sort_kpt;  /* keys per thread of the onesweep depth sort: 0 (= 12), 4, 8, 12 */
     int32_t pair_sort_kpt;   /* keys per thread of the onesweep pair sorts: 0 (= 12), 4, 8, 12 */
     int32_t coop_sort;       /* 0: sorts that fit run as one cooperative launch, 1: never */
-    int32_t reserved[4];
+    int32_t blend_schedule;  /* batched step's grey blends: 0, one block per tile; 1, resident
+                              * blocks take tiles from one work queue holding every view's
+                              * tiles, longest lists first */
+    int32_t reserved[3];
 } gsevt_tuning;
 
 /* Sizes of one rendering frame (host struct). */

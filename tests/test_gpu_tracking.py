@@ -371,12 +371,14 @@ def test_batched_sequence_tracker_matches_plain_tracker(threshold, tmp_path):
 
 
 @pytest.mark.parametrize("n", [20000, 200000])
-def test_blend_staging_with_tma_gather_matches_cp_async(n):
+def test_blend_staging_and_schedule_choices_agree(n):
     """The tracker blends staged with TMA tile::gather4 tensor copies (gsevt_tuning
-    blend_staging 2) give the images of the cp.async staging bit for bit and the same loss;
-    the twist gradients agree to FP32 atomic-order noise.  200k Gaussians at 320x240 make
-    tile lists of several 256-record batches, so the double buffering and the wait for an
-    issued batch when a block stops early both run."""
+    blend_staging 2) and / or run as resident blocks taking tiles from one longest-first
+    queue (blend_schedule 1) give the images of the default launch bit for bit and the same
+    loss; the twist gradients agree to FP32 atomic-order noise.  200k Gaussians at 320x240
+    make tile lists of several 256-record batches, so the double buffering, the wait for an
+    issued batch when a block stops early, and the mbarrier phases carried from tile to tile
+    in a resident block all run."""
     sc = synthetic.Scenario(n, 5, 320, 240, 300.0, 30000)
     m, cam = sc.map, sc.camera
     pk = pack_map(_t(m["xyz"]), _t(m["opacity"]), _t(m["sh"]), scales=_t(m["scale"]), rotations=_t(m["rot"]))
@@ -384,17 +386,19 @@ def test_blend_staging_with_tma_gather_matches_cp_async(n):
     E = rng.normal(size=cam.width * cam.height).astype(np.float32)
     E /= np.linalg.norm(E.astype(np.float64))
     out = []
-    for staging in (1, 2):
+    for staging, schedule in ((1, 0), (2, 0), (1, 1), (2, 1)):
         p = Problem(0, sc.init_R, sc.init_t, sc.init_lin, sc.init_ang, sc.delta_tau, cam.width, cam.height, cam.fx,
                     cam.fy, _t(E), lr=(0.0, 0.0, 0.0, 0.0), opt_vel=True)
-        bt = BatchedTracker([{"packed": pk, "n": n}], [p], device=DEV)
-        bt.frame.set_tuning(blend_staging=staging)
-        bt.step()
+        bt = BatchedTracker([{"packed": pk, "n": n}], [p], device=DEV, tuning="defaults")
+        bt.frame.set_tuning(blend_staging=staging, blend_schedule=schedule)
+        for _ in range(2):  # lr = 0: the second step repeats the first on reused buffers
+            bt.step()
         torch.cuda.synchronize()
         assert bt.check_status()[0] == 0
         out.append((bt.frame.image.clone(), bt.states()))
-    (img1, s1), (img2, s2) = out
-    assert torch.equal(img1.view(torch.int32), img2.view(torch.int32))
-    assert s1["loss"][0] == s2["loss"][0]
-    g1, g2 = s1["grad"][0], s2["grad"][0]
-    assert np.linalg.norm(g1 - g2) <= 1e-5 * np.linalg.norm(g1), (g1, g2)
+    img1, s1 = out[0]
+    for img2, s2 in out[1:]:
+        assert torch.equal(img1.view(torch.int32), img2.view(torch.int32))
+        assert s1["loss"][0] == s2["loss"][0]
+        g1, g2 = s1["grad"][0], s2["grad"][0]
+        assert np.linalg.norm(g1 - g2) <= 1e-5 * np.linalg.norm(g1), (g1, g2)
