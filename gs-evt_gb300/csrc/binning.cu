@@ -101,6 +101,107 @@ __device__ void scan_blocks(const uint32_t *sums, uint32_t *offs, int n, uint32_
     }
 }
 
+// ---- multi-block exclusive scan (for more block sums than one block scans quickly) ----
+// Three launches: 4096-element chunk sums, a one-block scan of the chunk sums (with the
+// total and the overflow check), and the per-chunk rescan that writes the offsets.  The
+// 64-bit chunk sums live in a scratch region (the sort-count table, free between sorts).
+#define SCAN_CHUNK 4096
+#define SCAN_SMALL 8192  // up to this many sums the one-block scan is used
+
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v, unsigned long long *wsum)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) wsum[w] = v;
+    __syncthreads();
+    unsigned long long t = 0;
+    if (w == 0) {
+        t = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;  // valid in warp 0
+}
+
+__global__ void __launch_bounds__(1024) k_scan_part(const uint32_t *sums, int n, unsigned long long *part)
+{
+    __shared__ unsigned long long wsum[32];
+    const int base = blockIdx.x * SCAN_CHUNK + 4 * (int)threadIdx.x;
+    unsigned long long s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (base + k < n) s += sums[base + k];
+    const unsigned long long t = block_sum_u64(s, wsum);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// exclusive scan of the chunk sums in place (one block), total and overflow flag; also
+// clears status[7] when asked (the filter's region cursor)
+__global__ void __launch_bounds__(1024) k_scan_top(unsigned long long *part, int nparts, uint32_t *total,
+                                                   uint32_t *status, uint32_t capacity, int clear_cursor)
+{
+    __shared__ unsigned long long wsc[32];
+    __shared__ unsigned long long carry;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (t == 0) carry = 0;
+    if (t == 0 && clear_cursor) status[7] = 0u;
+    __syncthreads();
+    for (int b0 = 0; b0 < nparts; b0 += 1024) {
+        const unsigned long long v = b0 + t < nparts ? part[b0 + t] : 0ull;
+        unsigned long long inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wsc[w] = inc;
+        __syncthreads();
+        unsigned long long wb = 0;
+        for (int i = 0; i < w; ++i) wb += wsc[i];
+        const unsigned long long c = carry;
+        if (b0 + t < nparts) part[b0 + t] = c + wb + inc - v;
+        __syncthreads();
+        if (t == 1023) carry = c + wb + inc;
+        __syncthreads();
+    }
+    if (t == 0) {
+        const unsigned long long tot = carry;
+        *total = (uint32_t)min(tot, 0xffffffffull);
+        if (capacity && tot > capacity) atomicOr(&status[0], GSEVT_STATUS_KEY_OVERFLOW);
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_final(const uint32_t *sums, int n, const unsigned long long *part,
+                                                     uint32_t *offs)
+{
+    __shared__ unsigned long long wsc[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int base = blockIdx.x * SCAN_CHUNK + 4 * (int)threadIdx.x;
+    uint32_t v[4];
+    unsigned long long s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        v[k] = base + k < n ? sums[base + k] : 0u;
+        s += v[k];
+    }
+    unsigned long long inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsc[w] = inc;
+    __syncthreads();
+    unsigned long long run = part[blockIdx.x] + inc - s;
+    for (int i = 0; i < w; ++i) run += wsc[i];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) offs[base + k] = (uint32_t)min(run, 0xffffffffull);
+        run += v[k];
+    }
+}
+
 __device__ __forceinline__ int find_view_by_sb(const gsevt_view *views, int num_views, int sb)
 {
     int lo = 0, hi = num_views - 1;
@@ -525,6 +626,26 @@ __global__ void k_ranges(const uint32_t *keys, const uint32_t *count_word, uint3
     }
 }
 
+// Exclusive scan of n block sums into offs, the total into *total (overflow flagged above
+// `capacity`, 0: no check): one block for small n, else the three-launch scan with its
+// chunk sums in the sort-count table.
+int scan_sums(const uint32_t *sums, uint32_t *offs, int n, uint32_t *total, const Workspace &ws, uint32_t capacity,
+              bool clear_cursor, cudaStream_t s)
+{
+    const int nparts = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    if (n <= SCAN_SMALL || (size_t)nparts * 8 > (size_t)(GS_COOP_GP + 1) * 256 * 4) {
+        if (clear_cursor) cudaMemsetAsync(ws.status + 7, 0, 4, s);
+        k_scan_blocks<<<1, 1024, 0, s>>>(sums, offs, n, total, ws.status, capacity);
+    } else {
+        unsigned long long *part = (unsigned long long *)ws.sort_hist;
+        k_scan_part<<<nparts, 1024, 0, s>>>(sums, n, part);
+        k_scan_top<<<1, 1024, 0, s>>>(part, nparts, total, ws.status, capacity, clear_cursor ? 1 : 0);
+        k_scan_final<<<nparts, 1024, 0, s>>>(sums, n, part, offs);
+    }
+    GS_CUDA_CHECK();
+    return GSEVT_OK;
+}
+
 BinParams make_params(const gsevt_frame *f, const Workspace &ws)
 {
     BinParams p;
@@ -572,7 +693,7 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
         cmp.num_scan_blocks = (uint32_t)L.num_scan_blocks;
         cmp.enabled = 1;
     } else {
-        k_scan_blocks<<<1, 1024, 0, s>>>(ws.vis_sums, ws.vis_offs, L.num_scan_blocks, ws.status + 5, ws.status, 0);
+        if (int st = scan_sums(ws.vis_sums, ws.vis_offs, L.num_scan_blocks, ws.status + 5, ws, 0, false, s)) return st;
         k_compact<<<L.num_scan_blocks, GS_BLOCK, 0, s>>>(p);
         GS_CUDA_CHECK();
     }
@@ -600,11 +721,16 @@ int gs_launch_depth_order(const gsevt_frame *f, const Workspace &ws, cudaStream_
     }
     if (coarse) {
         k_sorted_sums<true><<<nb, GS_BLOCK, 0, s>>>(p, ws.dvals[0]);
-        k_scan_blocks2<<<1, 1024, 0, s>>>(ws.tsums, ws.toffs, ws.status + 1, ws.csums, ws.coffs, ws.status + 6,
-                                          (int)nb, ws.status, L.key_capacity);
+        if ((int)nb <= SCAN_SMALL) {
+            k_scan_blocks2<<<1, 1024, 0, s>>>(ws.tsums, ws.toffs, ws.status + 1, ws.csums, ws.coffs, ws.status + 6,
+                                              (int)nb, ws.status, L.key_capacity);
+        } else {
+            if (int st = scan_sums(ws.tsums, ws.toffs, (int)nb, ws.status + 1, ws, L.key_capacity, true, s)) return st;
+            if (int st = scan_sums(ws.csums, ws.coffs, (int)nb, ws.status + 6, ws, L.key_capacity, false, s)) return st;
+        }
     } else {
         k_sorted_sums<false><<<nb, GS_BLOCK, 0, s>>>(p, ws.dvals[0]);
-        k_scan_blocks<<<1, 1024, 0, s>>>(ws.tsums, ws.toffs, (int)nb, ws.status + 1, ws.status, L.key_capacity);
+        if (int st = scan_sums(ws.tsums, ws.toffs, (int)nb, ws.status + 1, ws, L.key_capacity, false, s)) return st;
     }
     GS_CUDA_CHECK();
     return GSEVT_OK;

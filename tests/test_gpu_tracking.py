@@ -402,3 +402,51 @@ def test_blend_staging_and_schedule_choices_agree(n):
         assert s1["loss"][0] == s2["loss"][0]
         g1, g2 = s1["grad"][0], s2["grad"][0]
         assert np.linalg.norm(g1 - g2) <= 1e-5 * np.linalg.norm(g1), (g1, g2)
+
+
+def test_large_frames_run_the_multi_block_scans():
+    """Frames above 8192 scan blocks (here five 640x480 views of an 800k map, 4 M slots, and
+    three tracking problems of it, 4.8 M slots) compact and bin through the three-launch
+    block-sum scan instead of the one-block scan: every view of the frame is bit-exact
+    against the oracle, and each problem of the batched step has the loss it has when run
+    alone (which uses the cooperative sort)."""
+    from oracle import oracle
+    import helpers
+    n, W, H = 800_000, 640, 480
+    sc = synthetic.Scenario(n, 9, W, H, 600.0, 100000)
+    m, cam = sc.map, sc.camera
+    pk = pack_map(_t(m["xyz"]), _t(m["opacity"]), _t(m["sh"]), scales=_t(m["scale"]), rotations=_t(m["rot"]))
+    rng = np.random.default_rng(2)
+    poses = [synthetic.perturb(sc.gt_R, sc.gt_t, rng, 0.1, 5.0) for _ in range(5)]
+    views = [ViewSpec(W, H, 0, R=R, t=t, P=cam.proj, campos=gpose.campos(R, t), tanfovx=cam.tanfovx,
+                      tanfovy=cam.tanfovy) for R, t in poses]
+    fr = GSFrame([MapSpec(n, packed=pk)], views, channels=1, device=DEV)
+    assert fr.L.num_scan_blocks > 8192
+    fr.render(exact_keys=True)
+    torch.cuda.synchronize()
+    assert fr.status()[0] == 0
+    cov = helpers.cov6(m)
+    for i in (0, 4):
+        R, t = poses[i]
+        res = oracle.rasterize_view(m["xyz"], cov, m["sh"], m["opacity"], helpers.view_vector(R, t, cam), W, H,
+                                    [0.0], nch=1)
+        got = fr.pixels(i)[0].cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), res["image"][0].view(np.uint32)), i
+    del fr
+    E = rng.normal(size=W * H).astype(np.float32)
+    E /= np.linalg.norm(E.astype(np.float64))
+
+    def probs(sel):
+        return [Problem(0, poses[i][0], poses[i][1], sc.gt_lin, sc.gt_ang, sc.delta_tau, W, H, cam.fx, cam.fy, _t(E),
+                        lr=(0.0, 0.0, 0.0, 0.0), opt_vel=True) for i in sel]
+
+    big = BatchedTracker([{"packed": pk, "n": n}], probs([0, 1, 2]), device=DEV, tuning="defaults")
+    assert big.frame.L.num_scan_blocks > 8192
+    big.step()
+    torch.cuda.synchronize()
+    assert big.check_status()[0] == 0
+    lb = big.states()["loss"]
+    for k in range(3):
+        one = BatchedTracker([{"packed": pk, "n": n}], probs([k]), device=DEV, tuning="defaults")
+        one.step()
+        assert one.states()["loss"][0] == lb[k], k
