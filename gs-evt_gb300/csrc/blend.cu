@@ -59,6 +59,7 @@ struct BlendParams {
     float *image, *final_T, *depth, *alpha;
     int32_t *n_contrib, *n_touched;
     const float *dL_dimage, *dL_ddepth, *dL_dalpha;
+    int stage_all_warps;  // TMA staging: every warp issues its candidates' copies (staging 3)
     // persistent launches: the tiles in the order blocks take them, and the queue head
     const uint32_t *order;
     uint32_t *queue;
@@ -174,9 +175,9 @@ __device__ __forceinline__ void load_batch(const BlendParams &p, Batch<RGB> &buf
 // ---- TMA staging ----
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ void mbar_init(uint64_t *m)
+__device__ __forceinline__ void mbar_init(uint64_t *m, uint32_t count)
 {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(m)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(m)), "r"(count) : "memory");
 }
 
 __device__ __forceinline__ void mbar_arrive_expect(uint64_t *m, uint32_t bytes)
@@ -207,37 +208,45 @@ __device__ __forceinline__ void tma_gather4(void *dst, const CUtensorMap *tm, ui
                  : "memory");
 }
 
-// Warp 0 stages batch r of the tile range into buf: lane l takes the groups g = l and l + 32
-// of four candidates, reads their slot ids, stores them in buf.id, and (after lane 0 has
-// announced the batch's bytes on the mbarrier) copies their four records with one gather4
-// into the 128-byte group buf.r[4g .. 4g + 3].  Rows past the range repeat the batch's
-// first slot (copied but never read).  Called by all 32 lanes of warp 0.
+// Stages batch r of the tile range into buf with tile::gather4 copies, called by every
+// thread.  The issuing warps (warp 0 alone with staging 2; every warp for its own 32
+// candidates with staging 3) give each lane a group g of four candidates: the lane reads
+// their slot ids, stores them in buf.id, and (after the warp's lane 0 has announced the
+// warp's bytes on the mbarrier) copies their four records with one gather4 into the
+// 128-byte group buf.r[4g .. 4g + 3].  Rows past the range repeat the batch's first slot
+// (copied but never read); an issuing warp without rows still arrives, with no bytes.
 template <bool RGB>
 __device__ __forceinline__ void tma_load_batch(const BlendParams &p, Batch<RGB> &buf, uint2 range, int r,
                                                uint64_t *mbar, const CUtensorMap *tm)
 {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (!p.stage_all_warps && w != 0) return;
     const uint32_t base = range.x + (uint32_t)r * GS_BLOCK;
     const uint32_t n = min((uint32_t)GS_BLOCK, range.y - base);  // >= 1
     const uint32_t groups = (n + 3) / 4;
+    // this warp's groups: [g0, g1)
+    const uint32_t g0 = p.stage_all_warps ? 8u * (uint32_t)w : 0u;
+    const uint32_t g1 = min(groups, p.stage_all_warps ? g0 + 8u : 64u);
     const uint32_t first = __ldg(p.vals + base);
     uint32_t rows[2][4];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
+        const uint32_t g = g0 + (uint32_t)(lane + 32 * h);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const uint32_t c = 4 * (uint32_t)(lane + 32 * h) + (uint32_t)k;
-            rows[h][k] = c < n ? __ldg(p.vals + base + c) : first;
-            if (c < n) buf.id[c] = rows[h][k];
+            const uint32_t c = 4 * g + (uint32_t)k;
+            const bool own = g < g1 && c < n;
+            rows[h][k] = own ? __ldg(p.vals + base + c) : first;
+            if (own) buf.id[c] = rows[h][k];
         }
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive_expect(mbar, groups * 128u);
+    if (lane == 0) mbar_arrive_expect(mbar, (g1 > g0 ? g1 - g0 : 0u) * 128u);
     __syncwarp();
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        const uint32_t g = (uint32_t)(lane + 32 * h);
-        if (g < groups) tma_gather4(&buf.r[4 * g], tm, rows[h][0], rows[h][1], rows[h][2], rows[h][3], mbar);
+        const uint32_t g = g0 + (uint32_t)(lane + 32 * h);
+        if (g < g1) tma_gather4(&buf.r[4 * g], tm, rows[h][0], rows[h][1], rows[h][2], rows[h][3], mbar);
     }
 }
 
@@ -331,7 +340,7 @@ __device__ __forceinline__ void fwd_tile(const BlendParams &p, const CUtensorMap
     int issued = 0, waited = 0;  // TMA: batches issued / waited for
     if (rounds > 0) {
         if (TMA) {
-            if (threadIdx.x < 32) tma_load_batch(p, sb[0], range, 0, &mbar[0], tm);
+            tma_load_batch(p, sb[0], range, 0, &mbar[0], tm);
             issued = 1;
         } else {
             load_batch(p, sb[0], range, 0);
@@ -341,7 +350,7 @@ __device__ __forceinline__ void fwd_tile(const BlendParams &p, const CUtensorMap
         Batch<RGB> &cur = sb[r & 1];
         if (TMA) {
             if (r + 1 < rounds) {
-                if (threadIdx.x < 32) tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], tm);
+                tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], tm);
                 issued = r + 2;
             }
             if (!mbar_wait(&mbar[r & 1], (phase >> (r & 1)) & 1u, p.ws.spin_limit) && threadIdx.x == 0)
@@ -426,8 +435,10 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
     __shared__ int s_tile;
     if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
     if (TMA && threadIdx.x == 0) {
-        mbar_init(&mbar[0]);
-        mbar_init(&mbar[1]);
+        // one arrival per issuing warp: warp 0 (staging 2) or every warp (staging 3)
+        const uint32_t arrivals = p.stage_all_warps ? GS_BLOCK / 32 : 1;
+        mbar_init(&mbar[0], arrivals);
+        mbar_init(&mbar[1], arrivals);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     uint32_t phase = 0;  // TMA: parity of the next phase of each buffer's mbarrier (bit b)
@@ -623,7 +634,7 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
     int issued = 0, waited = 0;  // TMA: batches issued / waited for
     if (rounds > 0) {
         if (TMA) {
-            if (threadIdx.x < 32) tma_load_batch(p, sb[0], range, 0, &mbar[0], tm);
+            tma_load_batch(p, sb[0], range, 0, &mbar[0], tm);
             issued = 1;
         } else {
             load_batch(p, sb[0], range, 0);
@@ -633,7 +644,7 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
         Batch<RGB> &cur = sb[r & 1];
         if (TMA) {
             if (r + 1 < rounds) {
-                if (threadIdx.x < 32) tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], tm);
+                tma_load_batch(p, sb[(r + 1) & 1], range, r + 1, &mbar[(r + 1) & 1], tm);
                 issued = r + 2;
             }
             if (!mbar_wait(&mbar[r & 1], (phase >> (r & 1)) & 1u, p.ws.spin_limit) && threadIdx.x == 0)
@@ -796,8 +807,10 @@ __global__ void __launch_bounds__(GS_BLOCK, MODE == 0 ? 5 : 1) k_blend_bwd(Blend
     __shared__ int s_tile;
     if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
     if (TMA && threadIdx.x == 0) {
-        mbar_init(&mbar[0]);
-        mbar_init(&mbar[1]);
+        // one arrival per issuing warp: warp 0 (staging 2) or every warp (staging 3)
+        const uint32_t arrivals = p.stage_all_warps ? GS_BLOCK / 32 : 1;
+        mbar_init(&mbar[0], arrivals);
+        mbar_init(&mbar[1], arrivals);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     for (int i = threadIdx.x; i < GS_BLOCK * (NC + 1); i += GS_BLOCK) (&acc[0][0])[i] = 0.0f;
@@ -865,6 +878,7 @@ static BlendParams make_params(const gsevt_frame *f, const Workspace &ws, const 
     p.n_contrib = f->n_contrib;
     p.n_touched = f->n_touched;
     p.dL_dimage = p.dL_ddepth = p.dL_dalpha = nullptr;
+    p.stage_all_warps = f->L.tuning.blend_staging == 3;
     p.order = ws.keys[0];  // free once the tile lists are built (batched step)
     p.queue = ws.status + 8;
     p.num_tiles = f->L.total_tiles;
@@ -931,7 +945,8 @@ static bool record_tensor_map(const gsevt_frame *f, const Workspace &ws, CUtenso
 static bool use_tma(const gsevt_frame *f, const Workspace &ws, CUtensorMap *tm)
 {
     std::memset(tm, 0, sizeof(*tm));
-    return f->L.tuning.blend_staging == 2 && f->L.channels == 1 && record_tensor_map(f, ws, tm);
+    return (f->L.tuning.blend_staging == 2 || f->L.tuning.blend_staging == 3) && f->L.channels == 1 &&
+           record_tensor_map(f, ws, tm);
 }
 
 int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s,

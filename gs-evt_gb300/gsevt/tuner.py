@@ -7,13 +7,14 @@ candidate with CUDA events (median over `iters` replays, a buffer larger than L2
 between them) and keeps the fastest.  The search is a coordinate descent from the library
 defaults over
 
-    blend_staging    1 (cp.async per thread) | 2 (TMA tile::gather4, one warp per block)
+    blend_staging    1 (cp.async per thread) | 2 (TMA tile::gather4 issued by one warp) |
+                     3 (TMA tile::gather4 issued by every warp)
     depth_sort_kpt   4 | 8 | 12   keys per thread of the onesweep depth sort
     pair_sort_kpt    4 | 8 | 12   keys per thread of the onesweep (super-)tile sorts
     coop_sort        0 (one cooperative launch when the sort fits) | 1 (never)
     blend_schedule   0 (one block per tile) | 1 (resident blocks, one longest-first tile queue)
 
-(11 timings per pass, two passes).  Choices that a frame cannot use (the cooperative sort
+(12 timings per pass, two passes).  Choices that a frame cannot use (the cooperative sort
 of a frame above 8192 slots per SM, the onesweep passes of a sort that runs cooperatively)
 time alike and the defaults are kept for them.
 
@@ -30,7 +31,7 @@ import torch
 
 TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_table.json")
 DEFAULTS = {"blend_staging": 1, "depth_sort_kpt": 12, "pair_sort_kpt": 12, "coop_sort": 0, "blend_schedule": 0}
-SPACE = {"blend_staging": (1, 2), "blend_schedule": (0, 1), "depth_sort_kpt": (4, 8, 12), "pair_sort_kpt": (4, 8, 12),
+SPACE = {"blend_staging": (1, 2, 3), "blend_schedule": (0, 1), "depth_sort_kpt": (4, 8, 12), "pair_sort_kpt": (4, 8, 12),
          "coop_sort": (0, 1)}
 
 

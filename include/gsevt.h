@@ -141,7 +141,8 @@ typedef struct gsevt_pair {
 typedef struct gsevt_tuning {
     int32_t blend_staging;   /* how a blend block stages its batch of 256 records in shared
                               * memory: 0 or 1, one 16-byte cp.async per record half and thread;
-                              * 2, TMA tile::gather4 tensor copies issued by one warp (the grey
+                              * 2, TMA tile::gather4 tensor copies issued by one warp; 3, the
+                              * same issued by every warp for its 32 candidates (the grey
                               * tracker blends; the RGB drop-in blends always use cp.async) */
     int32_t depth_sort_kpt;  /* keys per thread of the onesweep depth sort: 0 (= 12), 4, 8, 12 */
     int32_t pair_sort_kpt;   /* keys per thread of the onesweep pair sorts: 0 (= 12), 4, 8, 12 */

@@ -386,7 +386,7 @@ def test_blend_staging_and_schedule_choices_agree(n):
     E = rng.normal(size=cam.width * cam.height).astype(np.float32)
     E /= np.linalg.norm(E.astype(np.float64))
     out = []
-    for staging, schedule in ((1, 0), (2, 0), (1, 1), (2, 1)):
+    for staging, schedule in ((1, 0), (2, 0), (3, 0), (1, 1), (2, 1), (3, 1)):
         p = Problem(0, sc.init_R, sc.init_t, sc.init_lin, sc.init_ang, sc.delta_tau, cam.width, cam.height, cam.fx,
                     cam.fy, _t(E), lr=(0.0, 0.0, 0.0, 0.0), opt_vel=True)
         bt = BatchedTracker([{"packed": pk, "n": n}], [p], device=DEV, tuning="defaults")
