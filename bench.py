@@ -688,6 +688,41 @@ def run_profile(args):
                       "keys": k, "status": st}))
 
 
+def run_profile_plain(args):
+    """The plain per-view drop-in path for a launch list: warmup + steps iterations of the
+    reference-structured loop (two rasterizer calls, torch grey / loss / autograd / Adam),
+    with each iteration's wall time and GPU time (CUDA events around it) printed, so that
+    the host share of an iteration can be read beside the kernel times."""
+    import torch
+    from gsevt.camera import Camera
+    from gsevt.renderer import GaussianMap
+    from gsevt.tracker import make_optimizer, plain_iteration
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    prob = build_problem(args.workload, dev)
+    sc, cam = prob["scenario"], prob["scenario"].camera
+    c = Camera(torch.tensor(sc.init_R, dtype=torch.float32), torch.tensor(sc.init_t, dtype=torch.float32),
+               torch.tensor(sc.init_ang, dtype=torch.float32), torch.tensor(sc.init_lin, dtype=torch.float32),
+               cam.fovx, cam.fovy, cam.width, cam.height, delta_tau=sc.delta_tau, device=dev)
+    c.fx, c.fy = cam.fx, cam.fy
+    gm = GaussianMap.from_synthetic(prob["map"], device=dev)
+    opt = make_optimizer(c, {"cam_rot_delta": 0.004, "cam_trans_delta": 0.004, "cam_w_delta": 0.002,
+                             "cam_v_delta": 0.002})
+    bg = torch.zeros(3, device=dev)
+    E = prob["E"].view(1, prob["H"], prob["W"])
+    rows = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        a.record()
+        plain_iteration(c, gm, bg, opt, 0, True, E, None)
+        b.record()
+        torch.cuda.synchronize()
+        rows.append({"iteration": i, "wall_ms": 1e3 * (time.perf_counter() - t0), "event_ms": a.elapsed_time(b)})
+    print(json.dumps({"mode": "profile-plain", "workload": args.workload, "iterations": rows}))
+
+
 def max_over_ranks(x, device):
     """Largest value of the float x over the ranks of the default process group (x when
     there is none): the job's time is its slowest replica's."""
@@ -721,7 +756,8 @@ def main():
     ap.add_argument("--tune-workload", action="append", default=None,
                     help="with --mode tune: workloads to tune (default: the headline, the 64 hypotheses and "
                          "the 16 sequences)")
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "sequence-tracking", "tune"],
+    ap.add_argument("--mode", default="bench",
+                    choices=["bench", "profile", "profile-plain", "sequence-tracking", "tune"],
                     help="profile: build the workload, then run warmup + steps un-graphed iterations "
                          "(for ncu launch lists; prints no timings)")
     args = ap.parse_args()
@@ -729,6 +765,8 @@ def main():
         return run_reference(args)
     if args.mode == "profile":
         return run_profile(args)
+    if args.mode == "profile-plain":
+        return run_profile_plain(args)
     if args.mode == "tune":
         return tune_workloads(args.tune_workload or ["adjoint-500k-640x480", "hypotheses-64x2-500k",
                                                      "sequences-16-uneven"])
