@@ -390,6 +390,42 @@ def run_sequence_tracking(dev, frames=10, count=16, window_s=0.025):
             "trajectory": "T(tau) = exp(sin(2 pi 0.2 tau) [0.5 m u, 20 deg k]), u, k unit axes per sequence"}
 
 
+def graph_kernel_count(bt):
+    """Kernel launches in one batched iteration, counted as the kernel nodes of a CUDA graph
+    capture of it (captured, not run; driver cuGraphGetNodes / cuGraphNodeGetType), or None
+    when this torch cannot keep the captured graph."""
+    import ctypes as C
+    import torch
+    try:
+        g = torch.cuda.CUDAGraph(keep_graph=True)
+    except TypeError:
+        return None
+    try:
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.graph(g, stream=s):
+            bt.step()
+        raw = C.c_void_p(g.raw_cuda_graph())
+        cu = C.CDLL("libcuda.so.1")
+        n = C.c_size_t(0)
+        if cu.cuGraphGetNodes(raw, None, C.byref(n)) != 0:
+            return None
+        nodes = (C.c_void_p * n.value)()
+        if cu.cuGraphGetNodes(raw, nodes, C.byref(n)) != 0:
+            return None
+        kernels = 0
+        for i in range(n.value):
+            t = C.c_int(-1)
+            if cu.cuGraphNodeGetType(C.c_void_p(nodes[i]), C.byref(t)) != 0:
+                return None
+            kernels += int(t.value == 0)  # CU_GRAPH_NODE_TYPE_KERNEL
+        return kernels
+    except Exception:
+        return None
+    finally:
+        torch.cuda.synchronize()
+
+
 def tune_workloads(names, iters=20, out=None):
     """Autotune the launch choices of each named workload on this GPU (gsevt.tuner) and
     write the table; prints one JSON line per workload."""
@@ -823,7 +859,8 @@ def main():
     # sorts by depth and builds the super-tile lists, or the depth sort (cooperative, or a
     # histogram and 4 onesweep passes), sorted sums, paired scan, coarse duplication and
     # the super-tile sort (histogram, passes, + a range kernel when there are two); then
-    # tile filter, blend fwd, loss, blend bwd, preprocess bwd, finalize
+    # tile filter, blend fwd (with the pair losses), blend bwd, twist adjoint (with the
+    # pose finish)
     L = bt.frame.L
     nsup = L.super_tiles if L.super_tiles > 0 else L.total_tiles // 4 + L.num_views + 1
     super_passes = (max(1, int(nsup - 1).bit_length()) + 7) // 8
@@ -832,9 +869,15 @@ def main():
     coop = L.num_vg <= coop_keys
     compact_launches = 0 if coop and L.num_scan_blocks * 256 <= coop_keys else 2
     if coop and super_passes == 1:
-        launches_per_iter = 8 + compact_launches
+        launches_per_iter = 6 + compact_launches
     else:
-        launches_per_iter = 11 + compact_launches + (1 if coop else 5) + super_passes + (1 if super_passes > 1 else 0)
+        launches_per_iter = 9 + compact_launches + (1 if coop else 5) + super_passes + (1 if super_passes > 1 else 0)
+    # the kernel nodes of a captured iteration, counted in the graph itself when torch can
+    # keep it (the estimate above otherwise)
+    counted = graph_kernel_count(bt)
+    launches_source = "estimate from the launch sequence"
+    if counted is not None:
+        launches_per_iter, launches_source = counted, "kernel nodes of the captured iteration graph"
     it_bytes = iteration_bytes(prob, dev)
     it_gbs = it_bytes["bytes_per_iter"] * (1000.0 / ms) / 1e9
     line = {
@@ -862,6 +905,7 @@ def main():
                                         "batched iterations/s of one GPU, against that GPU's HBM peak"),
         "counts": algo["counts"], "status": st,
         "gpu_launches": launches_per_iter * args.steps,
+        "gpu_launches_per_iteration": {"value": launches_per_iter, "source": launches_source},
         "clocks": clk,
     }
     if not args.no_secondary:
