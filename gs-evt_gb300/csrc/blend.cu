@@ -60,8 +60,6 @@ struct BlendParams {
     int32_t *n_contrib, *n_touched;
     const float *dL_dimage, *dL_ddepth, *dL_dalpha;
     int stage_all_warps;  // TMA staging: every warp issues its candidates' copies (staging 3)
-    int fuse_loss;        // batched step: the forward blend also forms the pair losses
-    double *loss_out;     // with fuse_loss: each pair's loss (nullable)
     // persistent launches: the tiles in the order blocks take them, and the queue head
     const uint32_t *order;
     uint32_t *queue;
@@ -266,93 +264,6 @@ __device__ __forceinline__ void tma_drain(uint64_t *mbar, uint32_t &phase, int i
     }
 }
 
-// The pair loss formed by the forward blend of the batched step (no separate loss launch).
-// The two blends of the same tile position of a pair's views take a ticket (the fourth
-// word of the pair tile's loss_part entry, after a fence); the second one adds, over the
-// tile's pixels, s2 = sum dI^2, cross = sum dI e (|dI| |e| unsigned) and e2 = sum e^2 (dI
-// linear or log grey, as in k_loss; its own pixel from registers, the other view's through
-// L2), as FP32 per pixel and float pairs per block, into that entry.  The last pair tile
-// of the pair (ticket on loss_done) adds the pair's tile entries in tile order and forms
-// the scalars exactly as k_loss does.  Results do not depend on which blend finishes
-// first or last.  Skipped views (finished problems) form nothing.
-__device__ __forceinline__ void pair_tile_loss(const BlendParams &p, const gsevt_view &V, int tile, bool inside,
-                                               int px, int py, float value)
-{
-    __shared__ int s_second, s_last;
-    __shared__ FP2 part[GS_BLOCK / 32][3];
-    __shared__ double dpart[GS_BLOCK / 32][3];
-    if (V.pair < 0 || V.skip) return;  // uniform
-    const gsevt_pair &pr = p.pairs[V.pair];
-    const gsevt_view &Vl = p.views[pr.last_view];
-    const int lt = tile - V.tile_offset;
-    const size_t key = (size_t)(Vl.tile_offset + lt);
-    uint32_t *ticket = (uint32_t *)(p.ws.loss_part + key * 4 + 3);
-    __threadfence();  // this tile's pixels are visible before the ticket
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        s_second = atomicAdd(ticket, 1u) == 1u;
-        if (s_second) *ticket = 0u;  // both blends have arrived: ready for the next iteration
-    }
-    __syncthreads();
-    if (!s_second) return;  // uniform
-    __threadfence();
-    float s2 = 0.0f, cr = 0.0f, e2 = 0.0f;
-    if (inside) {
-        const int lp = py * V.width + px;
-        const int other = V.pair_role == 0 ? pr.next_view : pr.last_view;
-        const float Io = __ldcg(p.image + p.views[other].pix_offset + lp);
-        const float In = V.pair_role == 0 ? Io : value, Il = V.pair_role == 0 ? value : Io;
-        const float d = pr.log_grey ? logf(In + pr.log_eps) - logf(Il + pr.log_eps) : In - Il;
-        const float e = (pr.unsigned_mode && pr.event_abs) ? __ldg(pr.event_abs + lp) : __ldg(pr.event + lp);
-        s2 = d * d;
-        e2 = e * e;
-        cr = pr.unsigned_mode ? fabsf(d) * fabsf(e) : d * e;
-    }
-    const FP2 S2 = warp_sum_fp2(s2), CR = warp_sum_fp2(cr), E2 = warp_sum_fp2(e2);
-    if ((threadIdx.x & 31) == 0) {
-        part[threadIdx.x >> 5][0] = S2;
-        part[threadIdx.x >> 5][1] = CR;
-        part[threadIdx.x >> 5][2] = E2;
-    }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-        FP2 t;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) t.add(part[w][threadIdx.x]);
-        p.ws.loss_part[key * 4 + threadIdx.x] = (double)t.hi + (double)t.lo;
-    }
-    __threadfence();
-    __syncthreads();
-    const int ntiles = Vl.tiles_x * Vl.tiles_y;
-    if (threadIdx.x == 0) s_last = atomicAdd(&p.ws.loss_done[V.pair], 1u) == (uint32_t)ntiles - 1u;
-    __syncthreads();
-    if (!s_last) return;  // uniform
-    __threadfence();
-    // the pair's tile entries in a fixed order: thread i adds tiles i, i + 256, ..., then a
-    // fixed-shape tree over the warps
-    const volatile double *lp = p.ws.loss_part + (size_t)Vl.tile_offset * 4;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (int i = threadIdx.x; i < ntiles; i += GS_BLOCK) {
-        a0 += lp[(size_t)i * 4];
-        a1 += lp[(size_t)i * 4 + 1];
-        a2 += lp[(size_t)i * 4 + 2];
-    }
-    a0 = warp_sum_d(a0);
-    a1 = warp_sum_d(a1);
-    a2 = warp_sum_d(a2);
-    if ((threadIdx.x & 31) == 0) {
-        dpart[threadIdx.x >> 5][0] = a0;
-        dpart[threadIdx.x >> 5][1] = a1;
-        dpart[threadIdx.x >> 5][2] = a2;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double S2t = 0, CRt = 0, E2t = 0;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) { S2t += dpart[w][0]; CRt += dpart[w][1]; E2t += dpart[w][2]; }
-        gs_pair_loss_scalars(p.ws, V.pair, S2t, CRt, E2t, p.loss_out);
-        p.ws.loss_done[V.pair] = 0u;
-    }
-}
-
 // Pixel of thread t: warps tile the 16x16 tile as 2 x 4 blocks of 8x4 pixels, so a warp's
 // footprint is nearly square (fewer Gaussians overlap it than a 16x2 strip).
 __device__ __forceinline__ void warp_pixel(int tid, int tx, int ty, int &px, int &py, float &sx0, float &sx1,
@@ -484,7 +395,6 @@ __device__ __forceinline__ void fwd_tile(const BlendParams &p, const CUtensorMap
     } else {
         cp_async_wait<0>();  // no copy may still target shared memory when the block exits
     }
-    float value = 0.0f;
     if (inside) {
         const int pix = V.pix_offset + py * V.width + px;
         const size_t P = (size_t)p.total_pixels;
@@ -494,8 +404,7 @@ __device__ __forceinline__ void fwd_tile(const BlendParams &p, const CUtensorMap
             p.image[2 * P + pix] = C2 + T * V.bg[2];
         } else {
             const float bgg = (0.2989f * V.bg[0] + 0.587f * V.bg[1]) + 0.114f * V.bg[2];
-            value = C0 + T * bgg;
-            p.image[pix] = value;
+            p.image[pix] = C0 + T * bgg;
         }
         p.final_T[pix] = T;
         if (EXTRAS) {
@@ -504,7 +413,6 @@ __device__ __forceinline__ void fwd_tile(const BlendParams &p, const CUtensorMap
             if (p.n_contrib) p.n_contrib[pix] = last;
         }
     }
-    if (!RGB && !EXTRAS && p.fuse_loss) pair_tile_loss(p, V, tile, inside, px, py, value);
 }
 
 // The next tile of a block, in thread 0: its own tile (one block per tile), or with
@@ -971,8 +879,6 @@ static BlendParams make_params(const gsevt_frame *f, const Workspace &ws, const 
     p.n_touched = f->n_touched;
     p.dL_dimage = p.dL_ddepth = p.dL_dalpha = nullptr;
     p.stage_all_warps = f->L.tuning.blend_staging == 3;
-    p.fuse_loss = 0;
-    p.loss_out = nullptr;
     p.order = ws.keys[0];  // free once the tile lists are built (batched step)
     p.queue = ws.status + 8;
     p.num_tiles = f->L.total_tiles;
@@ -1044,14 +950,10 @@ static bool use_tma(const gsevt_frame *f, const Workspace &ws, CUtensorMap *tm)
 }
 
 int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s,
-                        bool persist, bool fuse_loss, double *loss_out)
+                        bool persist)
 {
     if (f->L.total_tiles <= 0) return GSEVT_OK;
     BlendParams p = make_params(f, ws, vals);
-    // the batched step's grey pairs: the loss sums are formed by the blend itself
-    p.fuse_loss = fuse_loss && f->pairs && f->L.num_pairs > 0 && f->L.channels == 1 && !f->depth && !f->alpha &&
-                  !f->n_contrib && !f->n_touched;
-    p.loss_out = loss_out;
     if (f->n_touched) cudaMemsetAsync(f->n_touched, 0, (size_t)f->L.num_vg * 4, s);
     const int n = f->L.total_tiles;
     const bool extras = f->depth || f->alpha || f->n_contrib || f->n_touched;

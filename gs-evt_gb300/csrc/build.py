@@ -16,8 +16,9 @@ PKG = os.path.dirname(HERE)
 REPO = os.path.dirname(PKG)
 OUT_DIR = os.path.join(PKG, "gsevt", "_build")
 LIB = os.path.join(OUT_DIR, "libgsevt.so")
-SOURCES = ["preprocess.cu", "binning.cu", "sort.cu", "blend.cu", "loss.cu", "track.cu", "events.cu", "capi.cu"]
-CONTRACT = {"track.cu"}
+SOURCES = ["preprocess.cu", "preprocess_cached.cu", "binning.cu", "sort.cu", "blend.cu", "loss.cu", "track.cu",
+           "events.cu", "capi.cu"]
+CONTRACT = {"preprocess_cached.cu", "track.cu"}
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
          "-Xcompiler", "-fPIC", "-I", os.path.join(REPO, "include"), "-I", HERE]

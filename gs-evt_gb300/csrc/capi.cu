@@ -5,8 +5,7 @@
 #include "common.cuh"
 
 int gs_launch_preprocess_fwd(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
-int gs_launch_preprocess_bwd_cached(const gsevt_frame *f, const Workspace &ws, gsevt_pose_state *poses,
-                                    int num_poses, const double *loss, cudaStream_t s);
+int gs_launch_preprocess_bwd_cached(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
 int gs_launch_preprocess_bwd(const gsevt_frame *f, const Workspace &ws, const gsevt_map_grads *grads_dev,
                              double *xi_out, cudaStream_t s,
                              bool reduce);
@@ -16,12 +15,14 @@ int gs_launch_bin_coarse(const gsevt_frame *f, const Workspace &ws, uint32_t max
                          cudaStream_t s, bool binned);
 int gs_launch_bin(const gsevt_frame *f, const Workspace &ws, uint32_t max_keys, cudaStream_t s);
 int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, cudaStream_t s,
-                        bool persist = false, bool fuse_loss = false, double *loss_out = nullptr);
+                        bool persist = false);
 int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_t *vals, const float *dL_dimage,
                         const float *dL_ddepth, const float *dL_dalpha, cudaStream_t s, bool persist = false);
 bool gs_blend_persistent(const gsevt_frame *f);
 int gs_launch_tile_order(const gsevt_frame *f, const Workspace &ws, cudaStream_t s);
 int gs_launch_loss(const gsevt_frame *f, const Workspace &ws, double *loss_out, cudaStream_t s);
+int gs_launch_track_finalize(const gsevt_frame *f, const Workspace &ws, gsevt_pose_state *poses, int num_poses,
+                             const double *loss, cudaStream_t s);
 
 namespace {
 
@@ -63,11 +64,7 @@ extern "C" int gsevt_workspace_init(const gsevt_frame *f, gsevt_stream_t stream)
     gs_sort_prepare();
     cudaMemsetAsync(ws.status, 0, 64, s);
     cudaMemsetAsync(ws.sort_lookback, 0, (size_t)gs_lookback_tiles(f->L) * 256 * 8, s);
-    if (f->L.num_pairs > 0) {
-        cudaMemsetAsync(ws.loss_done, 0, (size_t)f->L.num_pairs * 4, s);
-        // the pair-tile tickets of the forward blend's loss sums (they reset themselves)
-        cudaMemsetAsync(ws.loss_part, 0, (size_t)std::max(f->L.loss_blocks, f->L.total_tiles) * 4 * 8, s);
-    }
+    if (f->L.num_pairs > 0) cudaMemsetAsync(ws.loss_done, 0, (size_t)f->L.num_pairs * 4, s);
     // tile and super-tile ranges always point inside the value buffers, even where a step
     // whose layout check failed (GSEVT_STATUS_LAYOUT) or whose sort gave up
     // (GSEVT_STATUS_SORT_TIMEOUT) leaves them unwritten
@@ -225,9 +222,9 @@ extern "C" int gsevt_track_step_batched(const gsevt_frame *f, gsevt_pose_state *
     if ((st = gs_launch_bin_coarse(f, ws, f->L.key_capacity, &fine, s, binned))) return st;
     const bool persist = gs_blend_persistent(f);
     if (persist && (st = gs_launch_tile_order(f, ws, s))) return st;
-    // the forward blend also forms the pair losses (its pair tiles' sums, then the scalars)
-    if ((st = gs_launch_blend_fwd(f, ws, fine, s, persist, true, loss_out))) return st;
+    if ((st = gs_launch_blend_fwd(f, ws, fine, s, persist))) return st;
+    if ((st = gs_launch_loss(f, ws, loss_out, s))) return st;
     if ((st = gs_launch_blend_bwd(f, ws, fine, nullptr, nullptr, nullptr, s, persist))) return st;
-    // the twist adjoint's last block per pose also runs the chain, Adam and the pose update
-    return gs_launch_preprocess_bwd_cached(f, ws, poses, num_poses, loss_out, s);
+    if ((st = gs_launch_preprocess_bwd_cached(f, ws, s))) return st;
+    return gs_launch_track_finalize(f, ws, poses, num_poses, loss_out, s);
 }

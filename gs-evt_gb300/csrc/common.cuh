@@ -103,7 +103,7 @@ struct Workspace {
     uint32_t *sort_counter;   // [GS_MAX_PASSES]
     unsigned long long *sort_lookback;  // [sort tiles][256]  {epoch:32 | flag:2 | count:30}
     uint2 *ranges;        // [total_tiles]
-    double *loss_part;    // [max(loss_blocks, total_tiles with pairs)][4]
+    double *loss_part;    // [loss_blocks][4]
     LossScal *loss_scal;  // [num_pairs] norms of the pair loss and the per-pixel gradient factors
     uint32_t *loss_done;  // [num_pairs]
     double *xi_part;      // [num_scan_blocks][6] float pairs (hi, lo) of the block's twist sums
@@ -203,9 +203,7 @@ inline Workspace gs_carve(const gsevt_layout &L, void *base)
     w.sort_counter = (uint32_t *)take(GS_MAX_PASSES * 4);
     w.sort_lookback = (unsigned long long *)take((size_t)gs_lookback_tiles(L) * 256 * 8);
     w.ranges = (uint2 *)take((size_t)L.total_tiles * 8);
-    // per loss block (k_loss) or, in the batched step, per pair tile: 3 FP64 sums and, in the
-    // fourth word of a pair tile's entry, the ticket of its two tiles' blends
-    w.loss_part = (double *)take((size_t)std::max(L.loss_blocks, L.num_pairs > 0 ? L.total_tiles : 0) * 4 * 8);
+    w.loss_part = (double *)take((size_t)L.loss_blocks * 4 * 8);
     w.loss_scal = (LossScal *)take((size_t)L.num_pairs * sizeof(LossScal));
     w.loss_done = (uint32_t *)take((size_t)L.num_pairs * 4);
     w.xi_part = (double *)take((size_t)L.num_scan_blocks * 6 * 8);
@@ -315,29 +313,6 @@ __device__ __forceinline__ double warp_sum_d(double v)
 // reports only failures of this call's own launches and copies.  (A sticky error, which
 // means the context is lost, is still reported by the next check.)
 #define GS_ENTRY() ((void)cudaGetLastError())
-
-// The loss scalars of pair pi from its sums s2 = sum dI^2, cross and e2 (one thread):
-// s = |dI|, L = sqrt(1 - 2 cross / s + e2), and the per-pixel gradient factors 1/s,
-// n.g = (1 - cross / s) / L and 1/L rounded to FP32 once, so that the adjoint blend's
-// per-pixel prologue stays in FP32; a non-finite L or s = 0 sets GSEVT_STATUS_NONFINITE.
-__device__ __forceinline__ void gs_pair_loss_scalars(const Workspace &ws, int pi, double S2t, double CRt, double E2t,
-                                                     double *loss_out)
-{
-    const double s = sqrt(S2t);
-    const double L2 = 1.0 - 2.0 * CRt / s + E2t;
-    const double L = sqrt(L2 > 0.0 ? L2 : 0.0);
-    LossScal &sc = ws.loss_scal[pi];
-    sc.s = s;
-    sc.cross = CRt;
-    sc.e2 = E2t;
-    sc.L = L;
-    sc.inv_s = (float)(1.0 / s);
-    sc.ndotg = (float)((1.0 - CRt / s) / L);
-    sc.inv_L = (float)(1.0 / L);
-    sc.pad = 0.0f;
-    if (loss_out) loss_out[pi] = L;
-    if (!(L == L) || !(s > 0.0)) atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
-}
 
 // Prepares the cooperative sort on the current device (sort.cu); outside stream capture.
 void gs_sort_prepare();

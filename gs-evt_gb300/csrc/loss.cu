@@ -49,9 +49,9 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     // FP32 sums over this thread's 8 pixels, FP64 from the warp level up
     float s2 = 0.0f, cr = 0.0f, e2 = 0.0f;
     const int base = lb * GS_BLOCK * LOSS_PIX_PER_THREAD;
+#pragma unroll
     const bool lg = pr.log_grey != 0;
     const float eps = pr.log_eps;
-#pragma unroll
     for (int k = 0; k < LOSS_PIX_PER_THREAD; ++k) {
         int i = base + k * GS_BLOCK + threadIdx.x;
         if (i < P) {
@@ -109,7 +109,22 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     if (threadIdx.x == 0) {
         double S2t = 0, CRt = 0, E2t = 0;
         for (int w = 0; w < GS_BLOCK / 32; ++w) { S2t += dpart[w][0]; CRt += dpart[w][1]; E2t += dpart[w][2]; }
-        gs_pair_loss_scalars(ws, pi, S2t, CRt, E2t, loss_out);
+        double s = sqrt(S2t);
+        double L2 = 1.0 - 2.0 * CRt / s + E2t;
+        double L = sqrt(L2 > 0.0 ? L2 : 0.0);
+        LossScal &sc = ws.loss_scal[pi];
+        sc.s = s;
+        sc.cross = CRt;
+        sc.e2 = E2t;
+        sc.L = L;
+        // factors of the per-pixel image gradient, rounded once here so the adjoint
+        // blend's per-pixel prologue stays in FP32
+        sc.inv_s = (float)(1.0 / s);
+        sc.ndotg = (float)((1.0 - CRt / s) / L);
+        sc.inv_L = (float)(1.0 / L);
+        sc.pad = 0.0f;
+        if (loss_out) loss_out[pi] = L;
+        if (!(L == L) || !(s > 0.0)) atomicOr(ws.status, GSEVT_STATUS_NONFINITE);
         ws.loss_done[pi] = 0u;
     }
 }

@@ -19,7 +19,7 @@
 // conic, cov2D, the Jacobian, the projection, depth and the SH view direction to (a) the
 // left-twist gradient of each view (warp-reduced in FP32, block sums as float pairs,
 // per-view sums in FP64) and (b) optionally the map gradients of the drop-in API.
-// The batched tracker's twist-only adjoint from the cache is in track.cu.
+// The batched tracker's twist-only adjoint from the cache is in preprocess_cached.cu.
 #include "common.cuh"
 
 namespace {
