@@ -859,8 +859,7 @@ def main():
     # sorts by depth and builds the super-tile lists, or the depth sort (cooperative, or a
     # histogram and 4 onesweep passes), sorted sums, paired scan, coarse duplication and
     # the super-tile sort (histogram, passes, + a range kernel when there are two); then
-    # tile filter, blend fwd (with the pair losses), blend bwd, twist adjoint (with the
-    # pose finish)
+    # tile filter, blend fwd, loss, blend bwd, twist adjoint, finalize
     L = bt.frame.L
     nsup = L.super_tiles if L.super_tiles > 0 else L.total_tiles // 4 + L.num_views + 1
     super_passes = (max(1, int(nsup - 1).bit_length()) + 7) // 8
@@ -869,9 +868,9 @@ def main():
     coop = L.num_vg <= coop_keys
     compact_launches = 0 if coop and L.num_scan_blocks * 256 <= coop_keys else 2
     if coop and super_passes == 1:
-        launches_per_iter = 6 + compact_launches
+        launches_per_iter = 8 + compact_launches
     else:
-        launches_per_iter = 9 + compact_launches + (1 if coop else 5) + super_passes + (1 if super_passes > 1 else 0)
+        launches_per_iter = 11 + compact_launches + (1 if coop else 5) + super_passes + (1 if super_passes > 1 else 0)
     # the kernel nodes of a captured iteration, counted in the graph itself when torch can
     # keep it (the estimate above otherwise)
     counted = graph_kernel_count(bt)

@@ -49,9 +49,9 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     // FP32 sums over this thread's 8 pixels, FP64 from the warp level up
     float s2 = 0.0f, cr = 0.0f, e2 = 0.0f;
     const int base = lb * GS_BLOCK * LOSS_PIX_PER_THREAD;
-#pragma unroll
     const bool lg = pr.log_grey != 0;
     const float eps = pr.log_eps;
+#pragma unroll
     for (int k = 0; k < LOSS_PIX_PER_THREAD; ++k) {
         int i = base + k * GS_BLOCK + threadIdx.x;
         if (i < P) {
