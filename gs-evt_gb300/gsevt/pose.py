@@ -88,4 +88,9 @@ def so3_log(R):
 
 
 def rotation_error_deg(Ra, Rb):
-    return math.degrees(np.linalg.norm(so3_log(Ra @ Rb.T)))
+    """Angle of Ra Rb^T in degrees, as atan2(sin, cos) of the relative rotation (the trace
+    alone loses angles below ~0.03 degrees to rounding when either matrix is FP32)."""
+    D = np.asarray(Ra, np.float64) @ np.asarray(Rb, np.float64).T
+    s = 0.5 * np.linalg.norm([D[2, 1] - D[1, 2], D[0, 2] - D[2, 0], D[1, 0] - D[0, 1]])
+    c = 0.5 * (np.trace(D) - 1.0)
+    return math.degrees(math.atan2(s, c))
