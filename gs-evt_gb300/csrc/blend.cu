@@ -30,7 +30,9 @@
 // ellipse_hits) and walks only those, in depth order, two at a time.  Gaussians that fail
 // both cannot pass the per-pixel alpha test, so the decisions and results are unchanged.
 // Every lane evaluates each candidate; the per-pixel decisions are predicates, not
-// divergent branches.
+// divergent branches.  The tracker adjoint's default form, k_blend_bwd_px2, gives each lane
+// two pixels (128 threads and 8x8-pixel warps per tile), so that one warp reduction serves
+// 64 pixels.
 //
 // Staging (gsevt_tuning.blend_staging): either every thread copies its candidate's 32-byte
 // record with two 16-byte cp.async, or (the grey tracker blends, staging 2) one warp stages
@@ -145,9 +147,10 @@ __device__ __forceinline__ bool ellipse_hits(float mx, float my, float4 E, float
 }
 
 // Which of the batch's candidates c0 + lane reach the warp's pixel rectangle (box overlap
-// and the ellipse test, both evaluated for every lane).
-template <bool RGB>
-__device__ __forceinline__ bool warp_hit(const Batch<RGB> &cur, int c0, int n, int lane, float sx0, float sx1,
+// and the ellipse test, both evaluated for every lane).  BT: a batch type with the
+// members r, box and ell.
+template <class BT>
+__device__ __forceinline__ bool warp_hit(const BT &cur, int c0, int n, int lane, float sx0, float sx1,
                                          float sy0, float sy1)
 {
     const int ci = min(c0 + lane, n - 1);
@@ -462,8 +465,10 @@ __global__ void __launch_bounds__(GS_BLOCK, RGB ? 5 : 6) k_blend_fwd(BlendParams
 // Modes: 0 tracker (grey, pose only: 0-4 and 6), 1 grey drop-in (0-7), 2 RGB drop-in (0-9).
 template <int MODE> struct Comps {
     static constexpr int n = MODE == 0 ? 6 : (MODE == 1 ? 8 : 10);
-    static constexpr int padded = MODE == 2 ? 16 : 8;  // power of two for the transposed reduction
 };
+// the component count rounded up to a power of two for the transposed reduction
+template <int MODE>
+__device__ __forceinline__ constexpr int comps_padded() { return MODE == 2 ? 16 : 8; }
 template <int MODE>
 __device__ __forceinline__ constexpr int comp_idx(int q) { return (MODE == 0 && q >= 5) ? 6 : q; }
 
@@ -496,13 +501,41 @@ __device__ __forceinline__ float warp_reduce_transposed(float (&v)[NV], int lane
     return v[0];
 }
 
+// Gradient of the pair loss w.r.t. pixel (px, py) of view V's grey image, whose value is
+// Is (V belongs to a pair: V.pair >= 0).
+__device__ __forceinline__ float pair_pixel_grad(const BlendParams &p, const gsevt_view &V, int px, int py, float Is)
+{
+    const gsevt_pair &pr = p.pairs[V.pair];
+    const LossScal &sc = p.ws.loss_scal[V.pair];
+    const float inv_s = sc.inv_s, ng = sc.ndotg, inv_L = sc.inv_L;
+    const int lp = py * V.width + px;
+    const int other = V.pair_role == 0 ? pr.next_view : pr.last_view;
+    const float Io = p.image[p.views[other].pix_offset + lp];
+    // log grey: dI of the logs, and dI/dI_self carries 1 / (I_self + eps)
+    const bool lg = pr.log_grey != 0;
+    const float ls = lg ? logf(Is + pr.log_eps) : Is, lo = lg ? logf(Io + pr.log_eps) : Io;
+    const float dI = V.pair_role == 0 ? (lo - ls) : (ls - lo);
+    const float e = (pr.unsigned_mode && pr.event_abs) ? pr.event_abs[lp] : pr.event[lp];
+    const float n = dI * inv_s;
+    float g;
+    if (pr.unsigned_mode) {
+        const float sg = (dI > 0.0f) ? 1.0f : (dI < 0.0f ? -1.0f : 0.0f);
+        g = sg * (fabsf(n) - fabsf(e)) * inv_L;
+    } else {
+        g = (n - e) * inv_L;
+    }
+    float dd = (g - n * ng) * inv_s;
+    if (lg) dd = __fdividef(dd, Is + pr.log_eps);
+    return V.pair_role == 0 ? -dd : dd;
+}
+
 // One candidate of the tracker adjoint (grey, pair-loss gradient gC per pixel): the
 // forward's decisions as predicates, the state update, and the six terms (the five
 // power-gradient moments and the colour gradient), zero for a lane that does not blend it.
-__device__ __forceinline__ bool tracker_candidate(const Batch<false> &cur, int j, float pxf, float pyf, float Cimg,
-                                                  float gC, float &T, float &Pc, bool &done, float (&g)[6])
+__device__ __forceinline__ bool tracker_candidate(const Rec *rec, int j, float pxf, float pyf, float Cimg, float gC,
+                                                  float &T, float &Pc, bool &done, float (&g)[6])
 {
-    const float4 A = cur.r[j].A, B = cur.r[j].B;
+    const float4 A = rec[j].A, B = rec[j].B;
     const float dx = A.x - pxf, dy = A.y - pyf;
     const float power = gs_power(B.x, B.y, B.z, dx, dy);
     const float araw = B.w * gs_expf(power);
@@ -602,30 +635,7 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
             if (p.dL_ddepth) { gD = p.dL_ddepth[pix]; Dtot = p.depth[pix]; }
             if (p.dL_dalpha) { gA = p.dL_dalpha[pix]; Atot = p.alpha[pix]; }
         } else if (V.pair >= 0) {
-            // gradient of the pair loss w.r.t. this view's grey image
-            const gsevt_pair &pr = p.pairs[V.pair];
-            const LossScal &sc = p.ws.loss_scal[V.pair];
-            const float inv_s = sc.inv_s, ng = sc.ndotg, inv_L = sc.inv_L;
-            const int lp = py * V.width + px;
-            const int other = V.pair_role == 0 ? pr.next_view : pr.last_view;
-            const float Io = p.image[p.views[other].pix_offset + lp];
-            const float Is = p.image[pix];
-            // log grey: dI of the logs, and dI/dI_self carries 1 / (I_self + eps)
-            const bool lg = pr.log_grey != 0;
-            const float ls = lg ? logf(Is + pr.log_eps) : Is, lo = lg ? logf(Io + pr.log_eps) : Io;
-            const float dI = V.pair_role == 0 ? (lo - ls) : (ls - lo);
-            const float e = (pr.unsigned_mode && pr.event_abs) ? pr.event_abs[lp] : pr.event[lp];
-            const float n = dI * inv_s;
-            float g;
-            if (pr.unsigned_mode) {
-                const float sg = (dI > 0.0f) ? 1.0f : (dI < 0.0f ? -1.0f : 0.0f);
-                g = sg * (fabsf(n) - fabsf(e)) * inv_L;
-            } else {
-                g = (n - e) * inv_L;
-            }
-            float dd = (g - n * ng) * inv_s;
-            if (lg) dd = __fdividef(dd, Is + pr.log_eps);
-            gC[0] = V.pair_role == 0 ? -dd : dd;
+            gC[0] = pair_pixel_grad(p, V, px, py, p.image[pix]);
         }
     }
 
@@ -680,9 +690,9 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
                     const int jb = has_b ? c0 + __ffs(mask) - 1 : ja;
                     if (has_b) mask &= mask - 1;
                     float ga[6], gb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-                    const bool ca = tracker_candidate(cur, ja, pxf, pyf, Cimg[0], gC[0], T, Pc[0], done, ga);
+                    const bool ca = tracker_candidate(cur.r, ja, pxf, pyf, Cimg[0], gC[0], T, Pc[0], done, ga);
                     bool cb = false;
-                    if (has_b) cb = tracker_candidate(cur, jb, pxf, pyf, Cimg[0], gC[0], T, Pc[0], done, gb);
+                    if (has_b) cb = tracker_candidate(cur.r, jb, pxf, pyf, Cimg[0], gC[0], T, Pc[0], done, gb);
                     if (__any_sync(0xffffffffu, ca || cb)) {
                         const float s = warp_reduce_pair6(ga, gb, lane);
                         const int q = (lane >> 1) & 7;
@@ -748,7 +758,7 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
                 gv[4] = my * dy;
                 T = contrib ? test_T : T;
                 if (__any_sync(0xffffffffu, contrib)) {
-                    constexpr int NV = Comps<MODE>::padded;
+                    constexpr int NV = comps_padded<MODE>();
                     constexpr int SH = NV == 8 ? 2 : 1;  // 5 - log2(NV)
                     float red[NV];
 #pragma unroll
@@ -827,6 +837,148 @@ __global__ void __launch_bounds__(GS_BLOCK, MODE == 0 ? 5 : 1) k_blend_bwd(Blend
         bwd_tile<MODE, TMA>(p, &tm, tile, sb, acc, V, mbar, phase);
         __syncthreads();  // V, s_tile and the batch buffers are reused by the next tile
     }
+}
+
+// ---- the tracker adjoint with two pixels per lane (gsevt_tuning.adjoint_pixels 0 or 2) ----
+// One block of 128 threads per tile: warp w covers the 8x8 pixel block (w & 1, w >> 1) of
+// the tile, lane l the pixels (l & 7, l >> 3) and (l & 7, (l >> 3) + 4) of it.  Each
+// candidate is evaluated for both pixels (each with its own transmittance, prefix and
+// stop state, in depth order as in the one-pixel adjoint), the two pixels' six terms are
+// added in the lane, and one warp reduction serves 64 pixels instead of 32.  The price is
+// the coarser warp culling (an 8x8 rectangle instead of two 8x4 ones) and half the warps
+// per tile.  Batches of 128 records halve the shared memory of a block (21 KB), so eight
+// blocks (32 warps, 64 registers a thread) are resident per SM against five blocks (40
+// warps) of the one-pixel adjoint.
+#define PX2_THREADS 128
+
+struct alignas(128) Batch2 {
+    Rec r[PX2_THREADS];
+    float4 box[PX2_THREADS];
+    float4 ell[PX2_THREADS];
+    uint32_t id[PX2_THREADS];
+};
+
+__device__ __forceinline__ void load_batch2(const BlendParams &p, Batch2 &buf, uint2 range, int r)
+{
+    const uint32_t idx = range.x + (uint32_t)r * PX2_THREADS + threadIdx.x;
+    if (idx < range.y) {
+        const uint32_t vg = __ldg(p.vals + idx);
+        buf.id[threadIdx.x] = vg;
+        cp_async16(&buf.r[threadIdx.x].A, p.ws.rec + 2 * (size_t)vg);
+        cp_async16(&buf.r[threadIdx.x].B, p.ws.rec + 2 * (size_t)vg + 1);
+    }
+    cp_async_commit();
+}
+
+__global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_bwd_px2(BlendParams p)
+{
+    constexpr int NC = Comps<0>::n;
+    __shared__ Batch2 sb[2];
+    __shared__ float acc[PX2_THREADS][NC + 1];
+    __shared__ gsevt_view V;
+    if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
+    const int tile = blockIdx.x;
+    if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
+    for (int i = threadIdx.x; i < PX2_THREADS * (NC + 1); i += PX2_THREADS) (&acc[0][0])[i] = 0.0f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lt = tile - V.tile_offset;
+    const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
+    const int bx = tx * GSEVT_TILE + (w & 1) * 8, by = ty * GSEVT_TILE + (w >> 1) * 8;
+    const int px = bx + (lane & 7), py0 = by + (lane >> 3), py1 = py0 + 4;
+    const float sx0 = (float)bx, sx1 = (float)(bx + 7), sy0 = (float)by, sy1 = (float)(by + 7);
+    const float pxf = (float)px, py0f = (float)py0, py1f = (float)py1;
+    const bool in0 = px < V.width && py0 < V.height, in1 = px < V.width && py1 < V.height;
+    float Cimg0 = 0.0f, gC0 = 0.0f, Cimg1 = 0.0f, gC1 = 0.0f;
+    if (in0) {
+        Cimg0 = p.image[V.pix_offset + py0 * V.width + px];
+        if (V.pair >= 0) gC0 = pair_pixel_grad(p, V, px, py0, Cimg0);
+    }
+    if (in1) {
+        Cimg1 = p.image[V.pix_offset + py1 * V.width + px];
+        if (V.pair >= 0) gC1 = pair_pixel_grad(p, V, px, py1, Cimg1);
+    }
+    const uint2 range = p.ws.ranges[tile];
+    const int todo = (int)(range.y - range.x);
+    const int rounds = (todo + PX2_THREADS - 1) / PX2_THREADS;
+    float T0 = 1.0f, T1 = 1.0f, P0 = 0.0f, P1 = 0.0f;
+    bool d0 = !in0, d1 = !in1;
+    if (rounds > 0) load_batch2(p, sb[0], range, 0);
+    for (int r = 0; r < rounds; ++r) {
+        Batch2 &cur = sb[r & 1];
+        if (r + 1 < rounds) {
+            load_batch2(p, sb[(r + 1) & 1], range, r + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        if (__syncthreads_count(d0 && d1) == PX2_THREADS) break;
+        const int n = min(PX2_THREADS, todo - r * PX2_THREADS);
+        if ((int)threadIdx.x < n) {
+            float4 e;
+            cur.box[threadIdx.x] = gauss_box(cur.r[threadIdx.x].A, cur.r[threadIdx.x].B, &e);
+            cur.ell[threadIdx.x] = e;
+        }
+        __syncthreads();
+        bool warp_done = false;
+        for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
+            const bool hit = warp_hit(cur, c0, n, lane, sx0, sx1, sy0, sy1);
+            unsigned mask = __ballot_sync(0xffffffffu, hit);
+            while (mask) {
+                if (__all_sync(0xffffffffu, d0 && d1)) { warp_done = true; break; }
+                const int ja = c0 + __ffs(mask) - 1;
+                mask &= mask - 1;
+                const bool has_b = mask != 0u;
+                const int jb = has_b ? c0 + __ffs(mask) - 1 : ja;
+                if (has_b) mask &= mask - 1;
+                float ga[6], gb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, h[6];
+                const bool ca0 = tracker_candidate(cur.r, ja, pxf, py0f, Cimg0, gC0, T0, P0, d0, ga);
+                const bool ca1 = tracker_candidate(cur.r, ja, pxf, py1f, Cimg1, gC1, T1, P1, d1, h);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) ga[k] += h[k];
+                bool cb = false;
+                if (has_b) {
+                    const bool cb0 = tracker_candidate(cur.r, jb, pxf, py0f, Cimg0, gC0, T0, P0, d0, gb);
+                    const bool cb1 = tracker_candidate(cur.r, jb, pxf, py1f, Cimg1, gC1, T1, P1, d1, h);
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) gb[k] += h[k];
+                    cb = cb0 || cb1;
+                }
+                if (__any_sync(0xffffffffu, ca0 || ca1 || cb)) {
+                    const float s = warp_reduce_pair6(ga, gb, lane);
+                    const int q = (lane >> 1) & 7;
+                    const bool second = (lane & 16) != 0;
+                    if ((lane & 1) == 0 && q < NC && s != 0.0f && (has_b || !second))
+                        atomicAdd(&acc[second ? jb : ja][q], s);
+                }
+            }
+        }
+        __syncthreads();
+        // this batch's per-Gaussian sums to the global per-slot gradients (the moments to
+        // the 2D mean and conic gradients, as in the one-pixel adjoint)
+        if ((int)threadIdx.x < n) {
+            const uint32_t vg = cur.id[threadIdx.x];
+            const float4 B = cur.r[threadIdx.x].B;
+            float *a = acc[threadIdx.x];
+            const float mx = a[0], my = a[1], mxx = a[2], mxy = a[3], myy = a[4];
+            a[0] = -(B.x * mx + B.y * my);
+            a[1] = -(B.z * my + B.y * mx);
+            a[2] = -0.5f * mxx;
+            a[3] = -mxy;
+            a[4] = -0.5f * myy;
+            float *dst[7] = {(float *)(p.ws.gradA + vg), (float *)(p.ws.gradA + vg) + 1, (float *)(p.ws.gradA + vg) + 2,
+                             (float *)(p.ws.gradA + vg) + 3, (float *)(p.ws.gradB + vg), (float *)(p.ws.gradB + vg) + 1,
+                             (float *)(p.ws.gradB + vg) + 2};
+#pragma unroll
+            for (int q = 0; q < NC; ++q) {
+                const float v = a[q];
+                if (v != 0.0f) atomicAdd(dst[comp_idx<0>(q)], v);
+                a[q] = 0.0f;
+            }
+        }
+        __syncthreads();
+    }
+    cp_async_wait<0>();  // no copy may still target shared memory when the block exits
 }
 
 // Orders the tiles for the persistent blends: descending list length in 33 buckets
@@ -997,6 +1149,8 @@ int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_
         k_blend_bwd<2, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
     } else if (dL_dimage) {
         k_blend_bwd<1, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+    } else if (f->L.tuning.adjoint_pixels != 1) {
+        k_blend_bwd_px2<<<n, PX2_THREADS, 0, s>>>(p);
     } else if (persist) {
         p.queue = ws.status + 9;
         if (tma) {

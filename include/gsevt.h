@@ -150,7 +150,12 @@ typedef struct gsevt_tuning {
     int32_t blend_schedule;  /* batched step's grey blends: 0, one block per tile; 1, resident
                               * blocks take tiles from one work queue holding every view's
                               * tiles, longest lists first */
-    int32_t reserved[3];
+    int32_t adjoint_pixels;  /* pixels per lane of the tracker adjoint blend: 0 or 2, two
+                              * (128 threads per tile, 8x8-pixel warps, batches of 128
+                              * records, cp.async staging and one block per tile whatever
+                              * blend_staging and blend_schedule say); 1, one (256 threads
+                              * per tile, 8x4-pixel warps, the staging and schedule above) */
+    int32_t reserved[2];
 } gsevt_tuning;
 
 /* Sizes of one rendering frame (host struct). */
