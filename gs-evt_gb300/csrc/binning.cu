@@ -486,8 +486,9 @@ __device__ __forceinline__ uint32_t cover_mask(uint32_t lo, uint32_t hi, int X, 
 }
 
 // One block per super-tile (16 warps, two blocks per SM); warp w takes the w-th
-// contiguous sixteenth of the super-tile's depth-ordered coarse list, four groups of 32
-// entries at a time (their loads in flight together).  Pass 1 counts, per warp and
+// contiguous sixteenth of the super-tile's depth-ordered coarse list: up to 16 groups of
+// 32 entries loaded at once and held in registers for both passes, or, for longer lists,
+// four groups at a time in each pass (their loads in flight together).  Pass 1 counts, per warp and
 // tile, the entries whose rectangle covers the tile; the block then claims a
 // contiguous region of the fine list with one atomic add and lays its 16 tile lists out
 // in it; pass 2 rescans the same entries and writes each one into the lists of the tiles
@@ -499,17 +500,20 @@ __device__ __forceinline__ uint32_t cover_mask(uint32_t lo, uint32_t hi, int X, 
 #define FILTER_TILES (GS_SUPER * GS_SUPER)
 #define FILTER_WARPS 16
 #define FILTER_ILP 4
+// entries per lane a warp holds in registers across the two passes (segments of at most
+// 32 * FILTER_REG entries are loaded once, all loads in flight together)
+#define FILTER_REG 16
+template <int G>
 __device__ __forceinline__ void filter_load(const uint32_t *cvals, const int4 *bin, uint32_t g, uint32_t b1,
-                                            int lane, int X, int Y, uint32_t (&vg)[FILTER_ILP],
-                                            uint32_t (&m)[FILTER_ILP])
+                                            int lane, int X, int Y, uint32_t (&vg)[G], uint32_t (&m)[G])
 {
 #pragma unroll
-    for (int k = 0; k < FILTER_ILP; ++k) {
+    for (int k = 0; k < G; ++k) {
         const uint32_t i = g + 32 * k + lane;
         vg[k] = i < b1 ? cvals[i] : 0xffffffffu;
     }
 #pragma unroll
-    for (int k = 0; k < FILTER_ILP; ++k) {
+    for (int k = 0; k < G; ++k) {
         m[k] = 0;
         if (vg[k] != 0xffffffffu) {
             const int4 b = bin[vg[k]];
@@ -518,7 +522,48 @@ __device__ __forceinline__ void filter_load(const uint32_t *cvals, const int4 *b
     }
 }
 
-__global__ void __launch_bounds__(FILTER_WARPS * 32) k_filter_tiles(const gsevt_view *views, int num_views,
+// Pass 1 for the first `groups` (warp-uniform) of G groups of 32 entries: per-tile counts
+// (lane t adds tile t's count to cnt).  Each lane spreads its 16-bit mask over four words,
+// one byte per tile (x * 0x00204081 moves bit i of a nibble to bit 8 i), so four warp-wide
+// integer sums count all 16 tiles at once (a group contributes at most 32 per byte).
+template <int G>
+__device__ __forceinline__ void filter_count(const uint32_t (&m)[G], int groups, int lane, uint32_t &cnt)
+{
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+        if (k < groups) {
+            uint32_t packed[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                packed[r] = __reduce_add_sync(0xffffffffu, (((m[k] >> (4 * r)) & 0xfu) * 0x00204081u) & 0x01010101u);
+            cnt += (packed[(lane >> 2) & 3] >> (8 * (lane & 3))) & 0xffu;
+        }
+    }
+}
+
+// Pass 2 for the first `groups` (warp-uniform) of G groups: each entry into the lists of
+// the tiles it covers (pos: the warp-uniform running position of each tile's list).
+template <int G>
+__device__ __forceinline__ void filter_write(const uint32_t (&vg)[G], const uint32_t (&m)[G], int groups,
+                                             uint32_t lt, uint32_t (&pos)[FILTER_TILES], uint32_t *fine_vals,
+                                             uint32_t capacity)
+{
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+        if (k < groups) {
+#pragma unroll
+            for (int t = 0; t < FILTER_TILES; ++t) {
+                const bool hit = (m[k] >> t) & 1u;
+                const uint32_t bal = __ballot_sync(0xffffffffu, hit);
+                const uint32_t at = pos[t] + __popc(bal & lt);
+                if (hit && at < capacity) fine_vals[at] = vg[k];
+                pos[t] += __popc(bal);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(FILTER_WARPS * 32, 2) k_filter_tiles(const gsevt_view *views, int num_views,
                                                                   Workspace ws, const uint32_t *cvals,
                                                                   uint32_t *fine_vals, uint32_t capacity)
 {
@@ -542,21 +587,22 @@ __global__ void __launch_bounds__(FILTER_WARPS * 32) k_filter_tiles(const gsevt_
     const uint32_t b0 = sr.x + min(len, (uint32_t)w * seg), b1 = sr.x + min(len, (uint32_t)(w + 1) * seg);
     const uint32_t lt = (1u << lane) - 1u;
 
-    // pass 1: per-tile counts of this warp's entries (lane t holds tile t's count).  Each
-    // lane spreads its 16-bit mask over four words, one byte per tile (x * 0x00204081
-    // moves bit i of a nibble to bit 8 i), so four warp-wide integer sums count all 16
-    // tiles at once (a group of 32 entries contributes at most 32 per byte).
+    // pass 1: per-tile counts of this warp's entries (lane t holds tile t's count).  A
+    // segment of at most 32 FILTER_REG entries (the same length for every warp of the block)
+    // is loaded once and kept in registers for pass 2; longer ones are loaded in steps of
+    // FILTER_ILP groups in each pass.
+    const bool in_regs = seg <= 32u * FILTER_REG;  // uniform over the block
+    const int rgroups = (int)((b1 - b0 + 31) / 32);
+    uint32_t rvg[FILTER_REG], rm[FILTER_REG];
     uint32_t cnt = 0;
-    for (uint32_t g = b0; g < b1; g += 32 * FILTER_ILP) {
-        uint32_t vg[FILTER_ILP], m[FILTER_ILP];
-        filter_load(cvals, ws.bin, g, b1, lane, X, Y, vg, m);
-#pragma unroll
-        for (int k = 0; k < FILTER_ILP; ++k) {
-            uint32_t packed[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-                packed[r] = __reduce_add_sync(0xffffffffu, (((m[k] >> (4 * r)) & 0xfu) * 0x00204081u) & 0x01010101u);
-            cnt += (packed[(lane >> 2) & 3] >> (8 * (lane & 3))) & 0xffu;
+    if (in_regs) {
+        filter_load<FILTER_REG>(cvals, ws.bin, b0, b1, lane, X, Y, rvg, rm);
+        filter_count<FILTER_REG>(rm, rgroups, lane, cnt);
+    } else {
+        for (uint32_t g = b0; g < b1; g += 32 * FILTER_ILP) {
+            uint32_t vg[FILTER_ILP], m[FILTER_ILP];
+            filter_load<FILTER_ILP>(cvals, ws.bin, g, b1, lane, X, Y, vg, m);
+            filter_count<FILTER_ILP>(m, FILTER_ILP, lane, cnt);
         }
     }
     if (lane < FILTER_TILES) s_cnt[w][lane] = cnt;
@@ -597,19 +643,13 @@ __global__ void __launch_bounds__(FILTER_WARPS * 32) k_filter_tiles(const gsevt_
     uint32_t pos[FILTER_TILES];
 #pragma unroll
     for (int t = 0; t < FILTER_TILES; ++t) pos[t] = s_start[t] + s_cnt[w][t];
-    for (uint32_t g = b0; g < b1; g += 32 * FILTER_ILP) {
-        uint32_t vg[FILTER_ILP], m[FILTER_ILP];
-        filter_load(cvals, ws.bin, g, b1, lane, X, Y, vg, m);
-#pragma unroll
-        for (int k = 0; k < FILTER_ILP; ++k) {
-#pragma unroll
-            for (int t = 0; t < FILTER_TILES; ++t) {
-                const bool hit = (m[k] >> t) & 1u;
-                const uint32_t bal = __ballot_sync(0xffffffffu, hit);
-                const uint32_t at = pos[t] + __popc(bal & lt);
-                if (hit && at < capacity) fine_vals[at] = vg[k];
-                pos[t] += __popc(bal);
-            }
+    if (in_regs) {
+        filter_write<FILTER_REG>(rvg, rm, rgroups, lt, pos, fine_vals, capacity);
+    } else {
+        for (uint32_t g = b0; g < b1; g += 32 * FILTER_ILP) {
+            uint32_t vg[FILTER_ILP], m[FILTER_ILP];
+            filter_load<FILTER_ILP>(cvals, ws.bin, g, b1, lane, X, Y, vg, m);
+            filter_write<FILTER_ILP>(vg, m, FILTER_ILP, lt, pos, fine_vals, capacity);
         }
     }
 }
