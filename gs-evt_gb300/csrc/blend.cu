@@ -30,9 +30,10 @@
 // ellipse_hits) and walks only those, in depth order, two at a time.  Gaussians that fail
 // both cannot pass the per-pixel alpha test, so the decisions and results are unchanged.
 // Every lane evaluates each candidate; the per-pixel decisions are predicates, not
-// divergent branches.  The tracker adjoint's default form, k_blend_bwd_px2, gives each lane
-// two pixels (128 threads and 8x8-pixel warps per tile), so that one warp reduction serves
-// 64 pixels.
+// divergent branches.  The default forms of the grey forward (k_blend_fwd_px2) and of the
+// tracker adjoint (k_blend_bwd_px2) give each lane two pixels (128 threads and 8x8-pixel
+// warps per tile): the two pixels share the record loads and loop control, and in the
+// adjoint one warp reduction serves 64 pixels.
 //
 // Staging (gsevt_tuning.blend_staging): either every thread copies its candidate's 32-byte
 // record with two 16-byte cp.async, or (the grey tracker blends, staging 2) one warp stages
@@ -870,6 +871,101 @@ __device__ __forceinline__ void load_batch2(const BlendParams &p, Batch2 &buf, u
     cp_async_commit();
 }
 
+// One candidate of the grey forward blend (no extras) for one pixel: the arithmetic of
+// fwd_candidate<false, false>, so the image bits are the same.
+__device__ __forceinline__ void grey_candidate(const Rec *rec, int j, float pxf, float pyf, float &T, float &C,
+                                               bool &done)
+{
+    const float4 A = rec[j].A, B = rec[j].B;
+    const float dx = A.x - pxf, dy = A.y - pyf;
+    const float power = gs_power(B.x, B.y, B.z, dx, dy);
+    const float alpha = fminf(0.99f, B.w * gs_expf(power));
+    const float test_T = T * (1.0f - alpha);
+    const bool pass = !done && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
+    const bool stop = pass && test_T < 0.0001f;
+    const bool use = pass && !stop;
+    done = done || stop;
+    C = use ? fmaf(A.w * alpha, T, C) : C;
+    T = use ? test_T : T;
+}
+
+// The grey forward blend of the batched step with two pixels per lane
+// (gsevt_tuning.forward_pixels 0 or 2): the layout of k_blend_bwd_px2 (128 threads and 8x8-pixel
+// warps per tile, batches of 128 records); every pixel runs the one-pixel forward's
+// sequence of operations, so images and transmittances are bit-identical.
+__global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_fwd_px2(BlendParams p)
+{
+    __shared__ Batch2 sb[2];
+    __shared__ gsevt_view V;
+    if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
+    const int tile = blockIdx.x;
+    if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lt = tile - V.tile_offset;
+    const int tx = lt % V.tiles_x, ty = lt / V.tiles_x;
+    const int bx = tx * GSEVT_TILE + (w & 1) * 8, by = ty * GSEVT_TILE + (w >> 1) * 8;
+    const int px = bx + (lane & 7), py0 = by + (lane >> 3), py1 = py0 + 4;
+    const float sx0 = (float)bx, sx1 = (float)(bx + 7), sy0 = (float)by, sy1 = (float)(by + 7);
+    const float pxf = (float)px, py0f = (float)py0, py1f = (float)py1;
+    const bool in0 = px < V.width && py0 < V.height, in1 = px < V.width && py1 < V.height;
+    const uint2 range = p.ws.ranges[tile];
+    const int todo = (int)(range.y - range.x);
+    const int rounds = (todo + PX2_THREADS - 1) / PX2_THREADS;
+    float T0 = 1.0f, T1 = 1.0f, C0 = 0.0f, C1 = 0.0f;
+    bool d0 = !in0, d1 = !in1;
+    if (rounds > 0) load_batch2(p, sb[0], range, 0);
+    for (int r = 0; r < rounds; ++r) {
+        Batch2 &cur = sb[r & 1];
+        if (r + 1 < rounds) {
+            load_batch2(p, sb[(r + 1) & 1], range, r + 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        if (__syncthreads_count(d0 && d1) == PX2_THREADS) break;
+        const int n = min(PX2_THREADS, todo - r * PX2_THREADS);
+        if ((int)threadIdx.x < n) {
+            float4 e;
+            cur.box[threadIdx.x] = gauss_box(cur.r[threadIdx.x].A, cur.r[threadIdx.x].B, &e);
+            cur.ell[threadIdx.x] = e;
+        }
+        __syncthreads();
+        bool warp_done = false;
+        for (int c0 = 0; c0 < n && !warp_done; c0 += 32) {
+            const bool hit = warp_hit(cur, c0, n, lane, sx0, sx1, sy0, sy1);
+            unsigned mask = __ballot_sync(0xffffffffu, hit);
+            // candidates two at a time (one saturation vote and loop step per pair)
+            while (mask) {
+                if (__all_sync(0xffffffffu, d0 && d1)) { warp_done = true; break; }
+                const int ja = c0 + __ffs(mask) - 1;
+                mask &= mask - 1;
+                grey_candidate(cur.r, ja, pxf, py0f, T0, C0, d0);
+                grey_candidate(cur.r, ja, pxf, py1f, T1, C1, d1);
+                if (mask) {
+                    const int jb = c0 + __ffs(mask) - 1;
+                    mask &= mask - 1;
+                    grey_candidate(cur.r, jb, pxf, py0f, T0, C0, d0);
+                    grey_candidate(cur.r, jb, pxf, py1f, T1, C1, d1);
+                }
+            }
+        }
+        __syncthreads();  // the next iteration overwrites this buffer
+    }
+    cp_async_wait<0>();  // no copy may still target shared memory when the block exits
+    const float bgg = (0.2989f * V.bg[0] + 0.587f * V.bg[1]) + 0.114f * V.bg[2];
+    if (in0) {
+        const int pix = V.pix_offset + py0 * V.width + px;
+        p.image[pix] = C0 + T0 * bgg;
+        p.final_T[pix] = T0;
+    }
+    if (in1) {
+        const int pix = V.pix_offset + py1 * V.width + px;
+        p.image[pix] = C1 + T1 * bgg;
+        p.final_T[pix] = T1;
+    }
+}
+
 __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_bwd_px2(BlendParams p)
 {
     constexpr int NC = Comps<0>::n;
@@ -1116,6 +1212,8 @@ int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_
         else k_blend_fwd<false, true, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
     } else if (extras) {
         k_blend_fwd<true, false, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
+    } else if (f->L.tuning.forward_pixels != 1) {
+        k_blend_fwd_px2<<<n, PX2_THREADS, 0, s>>>(p);
     } else if (persist) {
         p.queue = ws.status + 8;
         if (tma) {

@@ -83,7 +83,7 @@ class Pair(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("blend_staging", C.c_int32), ("depth_sort_kpt", C.c_int32), ("pair_sort_kpt", C.c_int32),
                 ("coop_sort", C.c_int32), ("blend_schedule", C.c_int32), ("adjoint_pixels", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("forward_pixels", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 class Layout(C.Structure):

@@ -261,7 +261,8 @@ class GSFrame:
 
     def set_tuning(self, **choices):
         """Launch choices (gsevt_tuning fields: blend_staging, depth_sort_kpt, pair_sort_kpt,
-        coop_sort, blend_schedule, adjoint_pixels); unnamed fields keep their values.  A CUDA
+        coop_sort, blend_schedule, adjoint_pixels, forward_pixels); unnamed fields keep their
+        values.  A CUDA
         graph captured before keeps the launches it recorded."""
         for k, v in choices.items():
             setattr(self.L.tuning, k, int(v))
@@ -270,7 +271,7 @@ class GSFrame:
     def tuning(self):
         t = self.L.tuning
         return {k: int(getattr(t, k)) for k in ("blend_staging", "depth_sort_kpt", "pair_sort_kpt", "coop_sort",
-                                                "blend_schedule", "adjoint_pixels")}
+                                                "blend_schedule", "adjoint_pixels", "forward_pixels")}
 
     def set_spin_limit(self, limit):
         """Polls a bounded device wait makes before it gives up (0: the library default)."""

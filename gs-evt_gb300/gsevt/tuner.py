@@ -14,8 +14,9 @@ defaults over
     coop_sort        0 (one cooperative launch when the sort fits) | 1 (never)
     blend_schedule   0 (one block per tile) | 1 (resident blocks, one longest-first tile queue)
     adjoint_pixels   2 (two pixels per lane of the tracker adjoint) | 1 (one pixel per lane)
+    forward_pixels   2 (two pixels per lane of the grey forward blend) | 1 (one pixel per lane)
 
-(13 timings per pass, two passes).  Choices that a frame cannot use (the cooperative sort
+(14 timings per pass, two passes).  Choices that a frame cannot use (the cooperative sort
 of a frame above 8192 slots per SM, the onesweep passes of a sort that runs cooperatively)
 time alike and the defaults are kept for them.
 
@@ -32,9 +33,9 @@ import torch
 
 TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_table.json")
 DEFAULTS = {"blend_staging": 1, "depth_sort_kpt": 12, "pair_sort_kpt": 12, "coop_sort": 0, "blend_schedule": 0,
-            "adjoint_pixels": 2}
-SPACE = {"blend_staging": (1, 2, 3), "blend_schedule": (0, 1), "adjoint_pixels": (2, 1), "depth_sort_kpt": (4, 8, 12),
-         "pair_sort_kpt": (4, 8, 12), "coop_sort": (0, 1)}
+            "adjoint_pixels": 2, "forward_pixels": 2}
+SPACE = {"blend_staging": (1, 2, 3), "blend_schedule": (0, 1), "adjoint_pixels": (2, 1), "forward_pixels": (2, 1),
+         "depth_sort_kpt": (4, 8, 12), "pair_sort_kpt": (4, 8, 12), "coop_sort": (0, 1)}
 
 
 def shape_key(layout):

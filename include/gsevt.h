@@ -155,7 +155,12 @@ typedef struct gsevt_tuning {
                               * records, cp.async staging and one block per tile whatever
                               * blend_staging and blend_schedule say); 1, one (256 threads
                               * per tile, 8x4-pixel warps, the staging and schedule above) */
-    int32_t reserved[2];
+    int32_t forward_pixels;  /* pixels per lane of the grey forward blend without extras (the
+                              * batched step): 0 or 2, two (128 threads per tile, 8x8-pixel
+                              * warps, batches of 128 records, cp.async staging, one block per
+                              * tile); 1, one (256 threads per tile, the staging and schedule
+                              * above); the images are the same bits either way */
+    int32_t reserved[1];
 } gsevt_tuning;
 
 /* Sizes of one rendering frame (host struct). */
