@@ -1,10 +1,12 @@
 // Per-tile front-to-back alpha blending and its adjoint.
 //
-// One block of 256 threads per 16x16 tile (global tile ids cover every view of the
-// frame, so views of different sizes share the launch).  The tile's depth-sorted
-// Gaussians are staged through shared memory in batches of 256 records (32 bytes
-// each, or 48 with RGB); a batch is loaded with cp.async (16-byte global->shared copies
-// that bypass registers) while the block is still blending the previous one.  A pixel
+// One block per 16x16 tile (global tile ids cover every view of the frame, so views of
+// different sizes share the launch): 256 threads, one pixel each, or 128 threads with two
+// pixels each (the grey forward and the tracker adjoint of the batched step, below).  The
+// tile's depth-sorted Gaussians are staged through shared memory in batches of one record
+// per thread (32 bytes each, or 48 with RGB); a batch is loaded with cp.async (16-byte
+// global->shared copies that bypass registers) while the block is still blending the
+// previous one.  A pixel
 // stops when its transmittance would fall below 1e-4; the block stops when
 // __syncthreads_count says every pixel has stopped.
 //
@@ -26,7 +28,7 @@
 //
 // Warp-level culling (both directions): each batch Gaussian gets a conservative pixel
 // box and quadratic form of its alpha support (gauss_box); a warp ballots which of them
-// reach its 8x4 pixel block (box overlap, then the exact ellipse-rectangle test of
+// reach its pixel block, 8x4 or 8x8 (box overlap, then the exact ellipse-rectangle test of
 // ellipse_hits) and walks only those, in depth order, two at a time.  Gaussians that fail
 // both cannot pass the per-pixel alpha test, so the decisions and results are unchanged.
 // Every lane evaluates each candidate; the per-pixel decisions are predicates, not

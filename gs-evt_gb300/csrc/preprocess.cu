@@ -244,13 +244,14 @@ __device__ __forceinline__ void sh_dir_grad(int deg, const float *w, float x, fl
 __device__ __forceinline__ void write_fcache(float4 *dst, const Pre &o, const float *cov, const float *sh,
                                              int sh_degree, bool has_col)
 {
+    // gradient-only quantities: fused multiply-adds (see sh_dir_grad)
     float T0S[3], T1S[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         const float Sj[3] = {cov[j == 0 ? 0 : (j == 1 ? 1 : 2)], cov[j == 0 ? 1 : (j == 1 ? 3 : 4)],
                              cov[j == 0 ? 2 : (j == 1 ? 4 : 5)]};
-        T0S[j] = o.T0[0] * Sj[0] + o.T0[1] * Sj[1] + o.T0[2] * Sj[2];
-        T1S[j] = o.T1[0] * Sj[0] + o.T1[1] * Sj[1] + o.T1[2] * Sj[2];
+        T0S[j] = fmaf(o.T0[2], Sj[2], fmaf(o.T0[1], Sj[1], o.T0[0] * Sj[0]));
+        T1S[j] = fmaf(o.T1[2], Sj[2], fmaf(o.T1[1], Sj[1], o.T1[0] * Sj[0]));
     }
     float U[3] = {0.0f, 0.0f, 0.0f};
     if (!has_col) {
@@ -258,13 +259,13 @@ __device__ __forceinline__ void write_fcache(float4 *dst, const Pre &o, const fl
                              o.rgb_raw[2] < 0.0f ? 0.0f : 0.114f};
         float gk[16];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) gk[k] = wc[0] * sh[3 * k] + wc[1] * sh[3 * k + 1] + wc[2] * sh[3 * k + 2];
+        for (int k = 0; k < 16; ++k) gk[k] = fmaf(wc[2], sh[3 * k + 2], fmaf(wc[1], sh[3 * k + 1], wc[0] * sh[3 * k]));
         float D[3];
         sh_dir_grad(sh_degree, gk, o.dir[0], o.dir[1], o.dir[2], D);
-        const float dd = o.dir[0] * D[0] + o.dir[1] * D[1] + o.dir[2] * D[2];
+        const float dd = fmaf(o.dir[2], D[2], fmaf(o.dir[1], D[1], o.dir[0] * D[0]));
         const float il = 1.0f / o.dirlen;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) U[j] = (D[j] - o.dir[j] * dd) * il;
+        for (int j = 0; j < 3; ++j) U[j] = fmaf(-o.dir[j], dd, D[j]) * il;
     }
     dst[0] = make_float4(o.cov2[0], o.cov2[1], o.cov2[2], o.det);
     dst[1] = make_float4(T0S[0], T0S[1], T0S[2], T1S[0]);
@@ -414,33 +415,59 @@ struct BwdParams {
 };
 
 // SH basis times weights: returns sum_k w[k] * dY_k/d(x,y,z) (x,y,z treated as free).
+// Gradient arithmetic only, so the terms are accumulated with explicit fused multiply-adds
+// (this file is otherwise compiled without contraction, for the forward's bit parity).
 __device__ __forceinline__ void sh_dir_grad(int deg, const float *w, float x, float y, float z, float *g)
 {
     const float C1 = 0.4886025119029199f;
     g[0] = g[1] = g[2] = 0.0f;
     if (deg < 1) return;
-    g[0] += -C1 * w[3];
-    g[1] += -C1 * w[1];
-    g[2] += C1 * w[2];
-    if (deg < 2) return;
-    const float C20 = 1.0925484305920792f, C21 = -1.0925484305920792f, C22 = 0.31539156525252005f,
-                C23 = -1.0925484305920792f, C24 = 0.5462742152960396f;
-    g[0] += C20 * y * w[4] - 2.0f * C22 * x * w[6] + C23 * z * w[7] + 2.0f * C24 * x * w[8];
-    g[1] += C20 * x * w[4] + C21 * z * w[5] - 2.0f * C22 * y * w[6] - 2.0f * C24 * y * w[8];
-    g[2] += C21 * y * w[5] + 4.0f * C22 * z * w[6] + C23 * x * w[7];
-    if (deg < 3) return;
-    const float C30 = -0.5900435899266435f, C31 = 2.890611442640554f, C32 = -0.4570457994644658f,
-                C33 = 0.3731763325901154f, C34 = -0.4570457994644658f, C35 = 1.445305721320277f,
-                C36 = -0.5900435899266435f;
-    float xx = x * x, yy = y * y, zz = z * z;
-    g[0] += C30 * 6.0f * x * y * w[9] + C31 * y * z * w[10] + C32 * (-2.0f * x * y) * w[11]
-            + C33 * (-6.0f * x * z) * w[12] + C34 * (4.0f * zz - 3.0f * xx - yy) * w[13]
-            + C35 * 2.0f * x * z * w[14] + C36 * (3.0f * xx - 3.0f * yy) * w[15];
-    g[1] += C30 * (3.0f * xx - 3.0f * yy) * w[9] + C31 * x * z * w[10]
-            + C32 * (4.0f * zz - xx - 3.0f * yy) * w[11] + C33 * (-6.0f * y * z) * w[12]
-            + C34 * (-2.0f * x * y) * w[13] + C35 * (-2.0f * y * z) * w[14] + C36 * (-6.0f * x * y) * w[15];
-    g[2] += C31 * x * y * w[10] + C32 * 8.0f * y * z * w[11] + C33 * (6.0f * zz - 3.0f * xx - 3.0f * yy) * w[12]
-            + C34 * 8.0f * x * z * w[13] + C35 * (xx - yy) * w[14];
+    float g0 = -C1 * w[3], g1 = -C1 * w[1], g2 = C1 * w[2];
+    if (deg >= 2) {
+        const float C20 = 1.0925484305920792f, C21 = -1.0925484305920792f, C22 = 0.31539156525252005f,
+                    C23 = -1.0925484305920792f, C24 = 0.5462742152960396f;
+        g0 = fmaf(C20 * y, w[4], g0);
+        g0 = fmaf((-2.0f * C22) * x, w[6], g0);
+        g0 = fmaf(C23 * z, w[7], g0);
+        g0 = fmaf((2.0f * C24) * x, w[8], g0);
+        g1 = fmaf(C20 * x, w[4], g1);
+        g1 = fmaf(C21 * z, w[5], g1);
+        g1 = fmaf((-2.0f * C22) * y, w[6], g1);
+        g1 = fmaf((-2.0f * C24) * y, w[8], g1);
+        g2 = fmaf(C21 * y, w[5], g2);
+        g2 = fmaf((4.0f * C22) * z, w[6], g2);
+        g2 = fmaf(C23 * x, w[7], g2);
+        if (deg >= 3) {
+            const float C30 = -0.5900435899266435f, C31 = 2.890611442640554f, C32 = -0.4570457994644658f,
+                        C33 = 0.3731763325901154f, C34 = -0.4570457994644658f, C35 = 1.445305721320277f,
+                        C36 = -0.5900435899266435f;
+            const float xx = x * x, yy = y * y, zz = z * z;
+            const float xy = x * y, xz = x * z, yz = y * z;
+            const float d3 = 3.0f * (xx - yy);
+            g0 = fmaf((6.0f * C30) * xy, w[9], g0);
+            g0 = fmaf(C31 * yz, w[10], g0);
+            g0 = fmaf((-2.0f * C32) * xy, w[11], g0);
+            g0 = fmaf((-6.0f * C33) * xz, w[12], g0);
+            g0 = fmaf(C34 * fmaf(4.0f, zz, fmaf(-3.0f, xx, -yy)), w[13], g0);
+            g0 = fmaf((2.0f * C35) * xz, w[14], g0);
+            g0 = fmaf(C36 * d3, w[15], g0);
+            g1 = fmaf(C30 * d3, w[9], g1);
+            g1 = fmaf(C31 * xz, w[10], g1);
+            g1 = fmaf(C32 * fmaf(4.0f, zz, fmaf(-3.0f, yy, -xx)), w[11], g1);
+            g1 = fmaf((-6.0f * C33) * yz, w[12], g1);
+            g1 = fmaf((-2.0f * C34) * xy, w[13], g1);
+            g1 = fmaf((-2.0f * C35) * yz, w[14], g1);
+            g1 = fmaf((-6.0f * C36) * xy, w[15], g1);
+            g2 = fmaf(C31 * xy, w[10], g2);
+            g2 = fmaf((8.0f * C32) * yz, w[11], g2);
+            g2 = fmaf(C33 * fmaf(6.0f, zz, -3.0f * (xx + yy)), w[12], g2);
+            g2 = fmaf((8.0f * C34) * xz, w[13], g2);
+            g2 = fmaf(C35 * (xx - yy), w[14], g2);
+        }
+    }
+    g[0] = g0;
+    g[1] = g1;
+    g[2] = g2;
 }
 
 __device__ __forceinline__ void sh_basis(int deg, float x, float y, float z, float *Y)
