@@ -306,6 +306,91 @@ def run_sequences(dev, flush, steps=10, warmup=3, count=16):
             "tuning": dict(bt.frame.tuning(), source=bt.tuning_source)}
 
 
+def run_sequence_compare(dev, which, frames=200, repeats=3, window_s=0.025):
+    """Long-sequence check of the tracker against the reference-structured loop: sequence i
+    of the 16-sequence workload (its map size, event count, resolution and trajectory; the
+    events are drawn again from a generator seeded 1000 + i) is tracked over `frames`
+    windows `repeats` times by BatchedSequenceTracker (alone in its launch) and once by the
+    plain per-view Tracker (torch Adam over the drop-in rasterizer, utils/tracker.py's
+    loop).  Reports each run's RMS and final drift and the first window whose error
+    exceeds 10 mm (not timed against anything; the plain loop takes minutes)."""
+    import torch
+    from gsevt import synthetic
+    from gsevt import pose as gpose
+    from gsevt.batched import BatchedSequenceTracker, DEFAULT_LR
+    from gsevt.camera import Camera
+    from gsevt.engine import GSFrame, MapSpec, ViewSpec, pack_map
+    from gsevt.events import EventArray
+    from gsevt.renderer import GaussianMap
+    from gsevt.tracker import Tracker
+    rng = np.random.default_rng(10)
+    res = [(346, 260), (640, 480), (1280, 720)]
+    params = []
+    for i in range(16):
+        n = int(np.exp(rng.uniform(np.log(5e4), np.log(1.5e6))))
+        ne = int(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        params.append((n, ne))
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    us = int(round(window_s * 1e6))
+    out = []
+    for i in which:
+        n, ne = params[i]
+        W, H = res[i % 3]
+        f = 600.0 * W / 640.0
+        m = synthetic.make_map(n, 10 + i)
+        pk = pack_map(t(m["xyz"]), t(m["opacity"]), t(m["sh"]), scales=t(m["scale"]), rotations=t(m["rot"]))
+        tr = synthetic.SinusoidTrajectory(10 + i)
+        cam = synthetic.PinholeCamera(W, H, f)
+        R0, t0 = tr.pose(0.0)
+        views = [ViewSpec(W, H, 0, R=R0, t=t0, P=cam.proj, campos=gpose.campos(R0, t0), tanfovx=cam.tanfovx,
+                          tanfovy=cam.tanfovy) for _ in range(2)]
+        fr = GSFrame([MapSpec(n, packed=pk)], views, channels=1, device=dev)
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(1000 + i)
+        wins = []
+        for k in range(frames):
+            for j, tau in enumerate((k * window_s, (k + 1) * window_s)):
+                fr.set_view_pose(j, *tr.pose(tau))
+            fr.render(exact_keys=True)
+            x, y, pol = synthetic.synth_events_device(fr.pixels(0)[0], fr.pixels(1)[0], ne, gen)
+            wins.append((x.cpu().numpy(), y.cpu().numpy(), pol.cpu().numpy(),
+                         np.array([k * us, (k + 1) * us], np.int64)))
+        del fr
+        R, tt = tr.pose(0.5 * window_s)
+        lv, av = tr.velocity(0.5 * window_s)
+
+        def drift(traj):
+            et = []
+            for k, (_, Rk, tk) in enumerate(traj):
+                Rg, tg = tr.pose((k + 0.5) * window_s)
+                et.append(float(np.linalg.norm(gpose.campos(Rk, tk) - gpose.campos(Rg, tg))))
+            return {"rms_drift_mm": 1e3 * float(np.sqrt(np.mean(np.square(et)))), "final_error_mm": 1e3 * et[-1],
+                    "first_window_over_10mm": next((k for k, e in enumerate(et) if e > 0.01), None)}
+        row = {"sequence": i, "resolution": "%dx%d" % (W, H), "gaussians": n, "events_per_window": ne, "batched": []}
+        for _ in range(repeats):
+            seq = BatchedSequenceTracker([{"packed": pk, "n": n}], [(0, W, H, f, f)], device=dev)
+            traj = seq.track([(R, tt, lv, av)], [[(w[0], w[1], w[2], w[3], None)] for w in wins])
+            row["batched"].append(dict(drift(traj[0]), adam_iterations=int(seq.iterations)))
+        cfg = {"Event": {"img_width": W, "img_height": H, "gaussian_kernel_size": 9,
+                         "intrinsic": {"data": [f, 0, W / 2, 0, f, H / 2, 0, 0, 1]},
+                         "distortion_factors": [0, 0, 0, 0, 0]},
+               "Optimizer": {"cam_rot_delta": DEFAULT_LR[0], "cam_trans_delta": DEFAULT_LR[1],
+                             "cam_w_delta": DEFAULT_LR[2], "cam_v_delta": DEFAULT_LR[3],
+                             "converged_threshold": 1e-4, "max_optim_iter": 200}}
+        c = Camera(torch.tensor(R, dtype=torch.float32), torch.tensor(tt, dtype=torch.float32),
+                   torch.tensor(av, dtype=torch.float32), torch.tensor(lv, dtype=torch.float32),
+                   cam.fovx, cam.fovy, W, H, delta_tau=window_s, device=dev)
+        c.fx, c.fy = cam.fx, cam.fy
+        ev = [EventArray(w[0], w[1], w[2], np.linspace(w[3][0], w[3][1], len(w[0])).astype(np.int64))
+              for w in wins]
+        trk = Tracker(cfg, ev, c, GaussianMap.from_synthetic(m, device=dev), None, torch.zeros(3, device=dev), dev)
+        row["plain"] = dict(drift(trk.tracking()), adam_iterations=int(trk.iterations))
+        out.append(row)
+        print(json.dumps(row), flush=True)
+    return {"mode": "sequence-compare", "frames": frames, "window_s": window_s, "sequences": out,
+            "trajectory": "T(tau) = exp(sin(2 pi 0.2 tau) [0.5 m u, 20 deg k]), u, k unit axes per sequence"}
+
+
 def run_sequence_tracking(dev, frames=10, count=16, window_s=0.025):
     """16 concurrent sequences tracked frame by frame along their own smooth trajectories:
     maps of 50k-1.5M Gaussians (log-uniform, seeds 10-25), sensors 346x260 / 640x480 /
@@ -789,11 +874,13 @@ def main():
                     help="skip the 64-hypothesis and 16-sequence workloads reported beside the headline")
     ap.add_argument("--sequence-frames", type=int, default=10,
                     help="frames each of the 16 sequences tracks in the sequence-tracking workload")
+    ap.add_argument("--compare-sequences", default="9,15",
+                    help="with --mode sequence-compare: indices of the 16 sequences to track with both loops")
     ap.add_argument("--tune-workload", action="append", default=None,
                     help="with --mode tune: workloads to tune (default: the headline, the 64 hypotheses and "
                          "the 16 sequences)")
     ap.add_argument("--mode", default="bench",
-                    choices=["bench", "profile", "profile-plain", "sequence-tracking", "tune"],
+                    choices=["bench", "profile", "profile-plain", "sequence-tracking", "sequence-compare", "tune"],
                     help="profile: build the workload, then run warmup + steps un-graphed iterations "
                          "(for ncu launch lists; prints no timings)")
     args = ap.parse_args()
@@ -806,6 +893,12 @@ def main():
     if args.mode == "tune":
         return tune_workloads(args.tune_workload or ["adjoint-500k-640x480", "hypotheses-64x2-500k",
                                                      "sequences-16-uneven"])
+    if args.mode == "sequence-compare":
+        import torch
+        torch.cuda.set_device(0)
+        which = [int(x) for x in args.compare_sequences.split(",") if x.strip()]
+        print(json.dumps(run_sequence_compare(torch.device("cuda", 0), which, frames=args.sequence_frames)))
+        return
     if args.mode == "sequence-tracking":
         import torch
         torch.cuda.set_device(0)

@@ -69,6 +69,7 @@ struct BlendParams {
     const uint32_t *order;
     uint32_t *queue;
     int num_tiles;
+    int ordered;  // two-pixel blends: block b takes tile order[b] (longest lists first)
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -900,7 +901,7 @@ __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_fwd_px2(BlendParams p)
     __shared__ Batch2 sb[2];
     __shared__ gsevt_view V;
     if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
-    const int tile = blockIdx.x;
+    const int tile = p.ordered ? (int)p.order[blockIdx.x] : (int)blockIdx.x;
     if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -975,7 +976,7 @@ __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_bwd_px2(BlendParams p)
     __shared__ float acc[PX2_THREADS][NC + 1];
     __shared__ gsevt_view V;
     if (gs_sort_timed_out(p.ws.status)) return;  // the tile lists are incomplete (uniform)
-    const int tile = blockIdx.x;
+    const int tile = p.ordered ? (int)p.order[blockIdx.x] : (int)blockIdx.x;
     if (threadIdx.x == 0) V = p.views[gs_find_view_by_tile(p.views, p.num_views, tile)];
     for (int i = threadIdx.x; i < PX2_THREADS * (NC + 1); i += PX2_THREADS) (&acc[0][0])[i] = 0.0f;
     __syncthreads();
@@ -1132,11 +1133,13 @@ static BlendParams make_params(const gsevt_frame *f, const Workspace &ws, const 
     p.order = ws.keys[0];  // free once the tile lists are built (batched step)
     p.queue = ws.status + 8;
     p.num_tiles = f->L.total_tiles;
+    p.ordered = 0;
     return p;
 }
 
-// Persistent blends (gsevt_tuning.blend_schedule 1, batched step only): the tile order and
-// the queue heads live in the first pair-key buffer and status words 8-9.
+// Longest-first blends (gsevt_tuning.blend_schedule 1, batched step only): the one-pixel
+// blends run persistent, the two-pixel blends launch one block per tile in that order; the
+// tile order and the queue heads live in the first pair-key buffer and status words 8-9.
 bool gs_blend_persistent(const gsevt_frame *f)
 {
     return f->L.tuning.blend_schedule == 1 && f->L.channels == 1 && (uint32_t)f->L.total_tiles <= f->L.key_capacity;
@@ -1215,6 +1218,7 @@ int gs_launch_blend_fwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     } else if (extras) {
         k_blend_fwd<true, false, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
     } else if (f->L.tuning.forward_pixels != 1) {
+        p.ordered = persist ? 1 : 0;  // the tile order was built for this launch
         k_blend_fwd_px2<<<n, PX2_THREADS, 0, s>>>(p);
     } else if (persist) {
         p.queue = ws.status + 8;
@@ -1250,6 +1254,7 @@ int gs_launch_blend_bwd(const gsevt_frame *f, const Workspace &ws, const uint32_
     } else if (dL_dimage) {
         k_blend_bwd<1, false, false><<<n, GS_BLOCK, 0, s>>>(p, tm);
     } else if (f->L.tuning.adjoint_pixels != 1) {
+        p.ordered = persist ? 1 : 0;
         k_blend_bwd_px2<<<n, PX2_THREADS, 0, s>>>(p);
     } else if (persist) {
         p.queue = ws.status + 9;

@@ -147,19 +147,20 @@ typedef struct gsevt_tuning {
     int32_t depth_sort_kpt;  /* keys per thread of the onesweep depth sort: 0 (= 12), 4, 8, 12 */
     int32_t pair_sort_kpt;   /* keys per thread of the onesweep pair sorts: 0 (= 12), 4, 8, 12 */
     int32_t coop_sort;       /* 0: sorts that fit run as one cooperative launch, 1: never */
-    int32_t blend_schedule;  /* batched step's grey blends: 0, one block per tile; 1, resident
-                              * blocks take tiles from one work queue holding every view's
-                              * tiles, longest lists first */
+    int32_t blend_schedule;  /* batched step's grey blends: 0, one block per tile in tile
+                              * order; 1, longest tile lists first: the one-pixel blends run
+                              * as resident blocks taking tiles from one work queue holding
+                              * every view's tiles, the two-pixel blends launch one block per
+                              * tile in that order */
     int32_t adjoint_pixels;  /* pixels per lane of the tracker adjoint blend: 0 or 2, two
                               * (128 threads per tile, 8x8-pixel warps, batches of 128
-                              * records, cp.async staging and one block per tile whatever
-                              * blend_staging and blend_schedule say); 1, one (256 threads
-                              * per tile, 8x4-pixel warps, the staging and schedule above) */
+                              * records, cp.async staging whatever blend_staging says); 1, one
+                              * (256 threads per tile, 8x4-pixel warps, the staging above) */
     int32_t forward_pixels;  /* pixels per lane of the grey forward blend without extras (the
                               * batched step): 0 or 2, two (128 threads per tile, 8x8-pixel
-                              * warps, batches of 128 records, cp.async staging, one block per
-                              * tile); 1, one (256 threads per tile, the staging and schedule
-                              * above); the images are the same bits either way */
+                              * warps, batches of 128 records, cp.async staging); 1, one (256
+                              * threads per tile, the staging above); the images are the same
+                              * bits either way */
     int32_t reserved[1];
 } gsevt_tuning;
 

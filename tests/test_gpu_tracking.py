@@ -375,8 +375,8 @@ def test_blend_staging_and_schedule_choices_agree(n, W, H):
     """The tracker blends staged with TMA tile::gather4 tensor copies (gsevt_tuning
     blend_staging 2) and / or run as resident blocks taking tiles from one longest-first
     queue (blend_schedule 1), and the tracker adjoint and the grey forward with two pixels
-    per lane (adjoint_pixels 2, forward_pixels 2), give the images of the one-pixel launch
-    bit for bit and the same
+    per lane (adjoint_pixels 2, forward_pixels 2; with blend_schedule 1 their blocks take
+    the tiles longest first), give the images of the one-pixel launch bit for bit and the same
     loss; the twist gradients agree to FP32 atomic-order noise.  200k Gaussians at 320x240
     make tile lists of several 256-record batches, so the double buffering, the wait for an
     issued batch when a block stops early, and the mbarrier phases carried from tile to tile
@@ -390,7 +390,8 @@ def test_blend_staging_and_schedule_choices_agree(n, W, H):
     E /= np.linalg.norm(E.astype(np.float64))
     out = []
     for staging, schedule, pixels, fpixels in ((1, 0, 1, 1), (2, 0, 1, 1), (3, 0, 1, 1), (1, 1, 1, 1), (2, 1, 1, 1),
-                                               (3, 1, 1, 1), (1, 0, 2, 1), (2, 1, 2, 1), (1, 0, 2, 2), (1, 0, 1, 2)):
+                                               (3, 1, 1, 1), (1, 0, 2, 1), (2, 1, 2, 1), (1, 0, 2, 2), (1, 0, 1, 2),
+                                               (1, 1, 2, 2)):
         p = Problem(0, sc.init_R, sc.init_t, sc.init_lin, sc.init_ang, sc.delta_tau, cam.width, cam.height, cam.fx,
                     cam.fy, _t(E), lr=(0.0, 0.0, 0.0, 0.0), opt_vel=True)
         bt = BatchedTracker([{"packed": pk, "n": n}], [p], device=DEV, tuning="defaults")
