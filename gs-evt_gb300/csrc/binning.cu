@@ -261,14 +261,17 @@ __global__ void __launch_bounds__(GS_BLOCK) k_compact(BinParams p)
     if (g < n) bin = p.ws.bin[vg];
     const uint32_t vis = bin.x > 0 ? 1u : 0u;
     const uint32_t c = p.ws.vis_offs[sb] + block_excl_scan(vis, wtot);
-    if (vis) {
-        p.ws.dkeys[0][c] = (uint32_t)bin.w;
-        p.ws.dvals[0][c] = (uint32_t)vg;
+    if (g < n) {
         // the adjoint blend accumulates into these with atomics: clear them here, in slot
-        // order (coalesced), for every slot that can receive a contribution
+        // order (coalesced), for every slot, so that a zero gradient also marks the slots
+        // the adjoint never reached (the cached twist adjoint skips them)
         p.ws.gradA[vg] = make_float4(0, 0, 0, 0);
         p.ws.gradB[vg] = make_float4(0, 0, 0, 0);
         if (p.rgb) p.ws.gradC[vg] = make_float4(0, 0, 0, 0);
+    }
+    if (vis) {
+        p.ws.dkeys[0][c] = (uint32_t)bin.w;
+        p.ws.dvals[0][c] = (uint32_t)vg;
     }
 }
 

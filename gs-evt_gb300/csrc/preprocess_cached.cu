@@ -38,10 +38,19 @@ __global__ void __launch_bounds__(GS_BLOCK) k_preprocess_bwd_cached(CachedParams
     float xi[6] = {0, 0, 0, 0, 0, 0};
     const int g = (b - V.sb_offset) * GS_BLOCK + threadIdx.x;
     const size_t vg = (size_t)V.vg_offset + g;
-    if (g < s_n && p.ws.bin[vg].x > 0) {
+    // The compaction cleared every slot's gradient, so a zero gradient marks a slot that is
+    // not visible or that the blend adjoint never reached (behind saturated pixels); its
+    // twist term is zero, and its forward cache (written for visible slots only) is not read.
+    float4 GA = make_float4(0.0f, 0.0f, 0.0f, 0.0f), GB = GA;
+    if (g < s_n) {
+        GA = p.ws.gradA[vg];
+        GB = p.ws.gradB[vg];
+    }
+    const bool live = GA.x != 0.0f || GA.y != 0.0f || GA.z != 0.0f || GA.w != 0.0f || GB.x != 0.0f ||
+                      GB.y != 0.0f || GB.z != 0.0f || GB.w != 0.0f;
+    if (live) {
         const float4 *c = p.ws.fcache + vg * GS_FCACHE;
         const float4 c0 = c[0], c1 = c[1], c2 = c[2], c3 = c[3], c4 = c[4], c5 = c[5];
-        const float4 GA = p.ws.gradA[vg], GB = p.ws.gradB[vg];
         const float gCa = GA.z, gCb = GA.w, gCc = GB.x;
         const float a2 = c0.x, b2 = c0.y, c2_ = c0.z, det = c0.w;
         const float d2 = det * det;

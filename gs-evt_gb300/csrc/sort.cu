@@ -527,14 +527,16 @@ __global__ void __launch_bounds__(GS_COOP_THREADS, 1) k_sort_coop(CoopParams p)
                     if (g < p.cmp.maps[V.map].n) {
                         const uint32_t vg = (uint32_t)V.vg_offset + (uint32_t)g;
                         const int4 b4 = p.cmp.bin[vg];
+                        // the adjoint blend accumulates into these with atomics; they are
+                        // cleared for every slot, so that a zero gradient also marks the
+                        // slots the adjoint never reached (the cached twist adjoint skips them)
+                        p.cmp.gradA[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        p.cmp.gradB[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        if (p.cmp.gradC) p.cmp.gradC[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                         if (b4.x > 0) {
                             v = true;
                             key[k] = (uint32_t)b4.w;
                             sin[li] = vg;
-                            // the adjoint blend accumulates into these with atomics
-                            p.cmp.gradA[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                            p.cmp.gradB[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                            if (p.cmp.gradC) p.cmp.gradC[vg] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                         }
                     }
                 }
