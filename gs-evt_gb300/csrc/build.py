@@ -17,7 +17,7 @@ REPO = os.path.dirname(PKG)
 OUT_DIR = os.path.join(PKG, "gsevt", "_build")
 LIB = os.path.join(OUT_DIR, "libgsevt.so")
 SOURCES = ["preprocess.cu", "preprocess_cached.cu", "binning.cu", "sort.cu", "blend.cu", "loss.cu", "track.cu",
-           "events.cu", "capi.cu"]
+           "events.cu", "ingest.cu", "capi.cu"]
 CONTRACT = {"preprocess_cached.cu", "track.cu"}
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
@@ -49,7 +49,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [NVCC, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", *objs, "-o", tmp, "-lcudart"]
+    cmd = [NVCC, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", *objs, "-o", tmp, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

@@ -11,6 +11,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libgsevt.so")
 
 GSEVT_OK = 0
+GSEVT_ERR_ARG = -1
+GSEVT_ERR_TOO_LARGE = -7
 ERRORS = {
     -1: "bad argument (shape, size or pointer)",
     -2: "key capacity overflow",
@@ -18,7 +20,7 @@ ERRORS = {
     -4: "bounded device wait ran out",
     -5: "CUDA launch or copy failed",
     -6: "workspace smaller than gsevt_workspace_bytes",
-    -7: "frame larger than the fixed scratch buffer holds",
+    -7: "input larger than the fixed scratch buffer or the given capacity holds",
 }
 STATUS_KEY_OVERFLOW = 1
 STATUS_SORT_TIMEOUT = 2
@@ -151,6 +153,8 @@ def lib():
                                               vp, vp, vp]),
         "gsevt_track_step_batched": (C.c_int, [fp, vp, i32, vp, vp]),
         "gsevt_track_init_views": (C.c_int, [vp, vp, i32, vp]),
+        "gsevt_parse_events_txt": (C.c_int, [C.c_char_p, C.c_size_t, vp, vp, vp, vp, C.c_size_t,
+                                             C.POINTER(C.c_size_t), i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -167,7 +171,7 @@ EXPORTED = [
     "gsevt_blend_bwd", "gsevt_preprocess_bwd", "gsevt_chain_view_grad", "gsevt_view_from_settings",
     "gsevt_read_status", "gsevt_clear_status", "gsevt_event_scratch_bytes",
     "gsevt_events_accumulate", "gsevt_events_accumulate_noalloc", "gsevt_track_step_batched",
-    "gsevt_track_init_views",
+    "gsevt_track_init_views", "gsevt_parse_events_txt",
 ]
 
 

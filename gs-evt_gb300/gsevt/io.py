@@ -116,21 +116,41 @@ def save_ply(path, xyz, features, opacity, scaling, rotation):
         f.write(table.tobytes())
 
 
+def parse_events_txt(text, threads=0):
+    """(ts int64, x uint16, y uint16, polarity uint8) arrays of an events.txt buffer, parsed
+    by the library's multi-threaded host parser (gsevt_parse_events_txt)."""
+    import ctypes as C
+    from . import _lib
+    buf = bytes(text)
+    cap = buf.count(b"\n") + 1
+    ts = np.empty(cap, np.int64)
+    x = np.empty(cap, np.uint16)
+    y = np.empty(cap, np.uint16)
+    pol = np.empty(cap, np.uint8)
+    n = C.c_size_t(0)
+    st = _lib.lib().gsevt_parse_events_txt(buf, len(buf), ts.ctypes.data, x.ctypes.data, y.ctypes.data,
+                                           pol.ctypes.data, cap, C.byref(n), int(threads))
+    if st != _lib.GSEVT_OK:
+        raise ValueError("events text: %s after %d events" % (_lib.ERRORS.get(st, "error %d" % st), n.value))
+    k = n.value
+    return ts[:k], x[:k], y[:k], pol[:k]
+
+
 def load_events_txt(path, max_events_per_frame, array_nums=None, start_time=None):
-    """Windows of max_events_per_frame events from "ts x y polarity" lines."""
+    """Windows of max_events_per_frame events from "ts x y polarity" lines: events before
+    start_time are skipped, the leftover events after the last full window are dropped,
+    and at most array_nums windows are returned (utils/event_camera/event.py:11-39)."""
     with open(path, "rb") as f:
-        data = np.array(f.read().split(), dtype=np.int64)
-    data = data.reshape(-1, 4)
+        ts, x, y, pol = parse_events_txt(f.read())
     if start_time is not None:
-        data = data[data[:, 0] >= start_time]
-    nwin = data.shape[0] // int(max_events_per_frame)
+        keep = ts >= start_time
+        ts, x, y, pol = ts[keep], x[keep], y[keep], pol[keep]
+    m = int(max_events_per_frame)
+    nwin = ts.shape[0] // m
     if array_nums is not None:
         nwin = min(nwin, int(array_nums))
-    out = []
-    for i in range(nwin):
-        d = data[i * max_events_per_frame:(i + 1) * max_events_per_frame]
-        out.append(EventArray(d[:, 1], d[:, 2], (d[:, 3] != 0).astype(np.uint8), d[:, 0]))
-    return out
+    return [EventArray(x[i * m:(i + 1) * m], y[i * m:(i + 1) * m], pol[i * m:(i + 1) * m], ts[i * m:(i + 1) * m])
+            for i in range(nwin)]
 
 
 def rotation_to_quaternion_xyzw(R):

@@ -324,11 +324,24 @@ int gsevt_events_accumulate(int64_t n, const uint16_t *x, const uint16_t *y,
  *     wait for the previous call to finish.
  * Outputs and every other argument are as for gsevt_events_accumulate. */
 #define GSEVT_EVENTS_NOALLOC_MAX_PIXELS (1280 * 720)
-enum { GSEVT_ERR_TOO_LARGE = -7 };  /* frame larger than a fixed-size scratch buffer holds */
+enum { GSEVT_ERR_TOO_LARGE = -7 };  /* input larger than a fixed-size scratch buffer, or an
+                                     * output capacity, holds */
 int gsevt_events_accumulate_noalloc(int64_t n, const uint16_t *x, const uint16_t *y,
                                     const uint8_t *polarity, int32_t width, int32_t height,
                                     const double *camera, int32_t ksize, int32_t levels,
                                     float *out_signed, float *out_unsigned, gsevt_stream_t stream);
+
+/* Event-file ingestion (replaces load_events_from_txt's line loop,
+ * utils/event_camera/event.py:11-39): parses a buffer holding the file's text, one event
+ * per line as "ts x y polarity" decimal integers separated by spaces or tabs, into host
+ * arrays ts[i] (the timestamp as written, microseconds), x[i], y[i] (0..65535) and
+ * polarity[i] = (p != 0).  Blank lines are skipped.  Host memory only: it launches
+ * nothing and needs no GPU.  capacity: entries of each output array, at least the number
+ * of lines in the buffer (GSEVT_ERR_TOO_LARGE otherwise, nothing parsed); threads: host
+ * threads to use (0: the hardware's count; buffers under 1 MB use one).  A line that is
+ * not four integers ends the parse with GSEVT_ERR_ARG and *count = the events before it. */
+int gsevt_parse_events_txt(const char *text, size_t len, int64_t *ts, uint16_t *x, uint16_t *y,
+                           uint8_t *polarity, size_t capacity, size_t *count, int32_t threads);
 
 /* ---- batched tracker iteration (utils/tracker.py:176-240) ----
  * Per pose state (one tracking hypothesis / sequence): FP64 pose, velocity, Adam

@@ -121,3 +121,58 @@ def test_png_round_trip(tmp_path):
     assert raw[:8] == b"\x89PNG\r\n\x1a\n" and raw[12:16] == b"IHDR"
     rgb = gio.read_png_rgb(p)
     np.testing.assert_array_equal(rgb, bgr[..., ::-1])
+
+
+def _parse_lines_python(text):
+    """Plain per-line restatement of the events.txt format for the parser tests."""
+    out = []
+    for line in text.decode().split("\n"):
+        tok = line.split()
+        if tok:
+            ts, x, y, p = (int(t) for t in tok)
+            out.append((ts, x, y, 1 if p != 0 else 0))
+    return out
+
+
+def test_native_event_parser_matches_line_parse():
+    """gsevt_parse_events_txt (host threads, no GPU) against a per-line parse: spaces and
+    tabs, CRLF line ends, blank lines, a last line without a newline, and a buffer large
+    enough for several threads, whose result does not depend on the thread count."""
+    rng = np.random.default_rng(3)
+    n = 120_000
+    ts = np.cumsum(rng.integers(0, 50, n)) + 10 ** 12
+    x, y, p = rng.integers(0, 1280, n), rng.integers(0, 720, n), rng.integers(-1, 2, n)
+    seps = [" ", "\t", "  "]
+    lines = []
+    for i in range(n):
+        s = rng.integers(0, 3)
+        lines.append(seps[s].join(str(int(v)) for v in (ts[i], x[i], y[i], p[i])) + ("\r" if i % 7 == 0 else ""))
+        if i % 1000 == 0:
+            lines.append("   ")
+    text = "\n".join(lines).encode()  # no newline after the last line
+    assert len(text) > (1 << 20)
+    ref = np.array(_parse_lines_python(text), np.int64)
+    for threads in (1, 3, 8):
+        got = gio.parse_events_txt(text, threads=threads)
+        assert got[0].shape[0] == n
+        assert np.array_equal(got[0], ref[:, 0]) and np.array_equal(got[1], ref[:, 1])
+        assert np.array_equal(got[2], ref[:, 2]) and np.array_equal(got[3], ref[:, 3])
+        assert got[1].dtype == np.uint16 and got[3].dtype == np.uint8
+
+
+def test_native_event_parser_rejects_malformed_lines():
+    import ctypes as C
+    from gsevt import _lib
+    good = b"1 2 3 1\n4 5 6 0\n"
+    for bad in (b"7 8 9\n", b"7 8 9 1 5\n", b"7 x 9 1\n", b"7 70000 9 1\n", b"7 -1 9 1\n"):
+        with pytest.raises(ValueError, match="after 2 events"):
+            gio.parse_events_txt(good + bad + good)
+    # an output capacity below the line count is refused before parsing
+    ts = np.empty(1, np.int64)
+    xy = np.empty(1, np.uint16)
+    pol = np.empty(1, np.uint8)
+    cnt = C.c_size_t(5)
+    st = _lib.lib().gsevt_parse_events_txt(good, len(good), ts.ctypes.data, xy.ctypes.data, xy.ctypes.data,
+                                           pol.ctypes.data, 1, C.byref(cnt), 0)
+    assert st == _lib.GSEVT_ERR_TOO_LARGE and cnt.value == 0
+    assert gio.parse_events_txt(b"")[0].shape == (0,)
