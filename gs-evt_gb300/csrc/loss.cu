@@ -19,7 +19,10 @@
 
 namespace {
 
-#define LOSS_PIX_PER_THREAD 8
+// threads of a loss block and pixels per thread (GSEVT_LOSS_PIXELS_PER_BLOCK = their product)
+#define LOSS_THREADS 512
+#define LOSS_PIX_PER_THREAD 4
+static_assert(LOSS_THREADS * LOSS_PIX_PER_THREAD == GSEVT_LOSS_PIXELS_PER_BLOCK, "loss block size");
 
 __device__ __forceinline__ int find_pair(const gsevt_pair *pairs, int num_pairs, int block)
 {
@@ -31,11 +34,11 @@ __device__ __forceinline__ int find_pair(const gsevt_pair *pairs, int num_pairs,
     return lo;
 }
 
-__global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, const gsevt_pair *pairs, int num_pairs,
+__global__ void __launch_bounds__(LOSS_THREADS) k_loss(const gsevt_view *views, const gsevt_pair *pairs, int num_pairs,
                                                    const float *image, Workspace ws, double *loss_out)
 {
-    __shared__ FP2 part[GS_BLOCK / 32][3];
-    __shared__ double dpart[GS_BLOCK / 32][3];
+    __shared__ FP2 part[LOSS_THREADS / 32][3];
+    __shared__ double dpart[LOSS_THREADS / 32][3];
     __shared__ bool is_last;
     if (gs_sort_timed_out(ws.status)) return;  // no images were rendered (uniform)
     const int b = blockIdx.x;
@@ -48,12 +51,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     const int lb = b - pr.block_offset;
     // FP32 sums over this thread's 8 pixels, FP64 from the warp level up
     float s2 = 0.0f, cr = 0.0f, e2 = 0.0f;
-    const int base = lb * GS_BLOCK * LOSS_PIX_PER_THREAD;
+    const int base = lb * LOSS_THREADS * LOSS_PIX_PER_THREAD;
     const bool lg = pr.log_grey != 0;
     const float eps = pr.log_eps;
 #pragma unroll
     for (int k = 0; k < LOSS_PIX_PER_THREAD; ++k) {
-        int i = base + k * GS_BLOCK + threadIdx.x;
+        int i = base + k * LOSS_THREADS + threadIdx.x;
         if (i < P) {
             const float In = image[Vn.pix_offset + i], Il = image[Vl.pix_offset + i];
             float d = lg ? logf(In + eps) - logf(Il + eps) : In - Il;
@@ -74,7 +77,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     __syncthreads();
     if (threadIdx.x < 3) {
         FP2 t;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) t.add(part[w][threadIdx.x]);
+        for (int w = 0; w < LOSS_THREADS / 32; ++w) t.add(part[w][threadIdx.x]);
         ws.loss_part[(size_t)b * 4 + threadIdx.x] = (double)t.hi + (double)t.lo;
     }
     __threadfence();
@@ -90,7 +93,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     // a fixed order, then a fixed-shape tree, so the result does not depend on scheduling
     const volatile double *lp = ws.loss_part;
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (int i = threadIdx.x; i < pr.num_blocks; i += GS_BLOCK) {
+    for (int i = threadIdx.x; i < pr.num_blocks; i += LOSS_THREADS) {
         size_t q = (size_t)(pr.block_offset + i) * 4;
         a0 += lp[q];
         a1 += lp[q + 1];
@@ -108,7 +111,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
     __syncthreads();
     if (threadIdx.x == 0) {
         double S2t = 0, CRt = 0, E2t = 0;
-        for (int w = 0; w < GS_BLOCK / 32; ++w) { S2t += dpart[w][0]; CRt += dpart[w][1]; E2t += dpart[w][2]; }
+        for (int w = 0; w < LOSS_THREADS / 32; ++w) { S2t += dpart[w][0]; CRt += dpart[w][1]; E2t += dpart[w][2]; }
         double s = sqrt(S2t);
         double L2 = 1.0 - 2.0 * CRt / s + E2t;
         double L = sqrt(L2 > 0.0 ? L2 : 0.0);
@@ -131,12 +134,12 @@ __global__ void __launch_bounds__(GS_BLOCK) k_loss(const gsevt_view *views, cons
 
 }  // namespace
 
-int gs_loss_blocks_for(int pixels) { return (pixels + GS_BLOCK * LOSS_PIX_PER_THREAD - 1) / (GS_BLOCK * LOSS_PIX_PER_THREAD); }
+int gs_loss_blocks_for(int pixels) { return (pixels + LOSS_THREADS * LOSS_PIX_PER_THREAD - 1) / (LOSS_THREADS * LOSS_PIX_PER_THREAD); }
 
 int gs_launch_loss(const gsevt_frame *f, const Workspace &ws, double *loss_out, cudaStream_t s)
 {
     if (f->L.num_pairs <= 0 || f->L.loss_blocks <= 0 || !f->pairs) return GSEVT_ERR_ARG;
-    k_loss<<<f->L.loss_blocks, GS_BLOCK, 0, s>>>(f->views, f->pairs, f->L.num_pairs, f->image, ws, loss_out);
+    k_loss<<<f->L.loss_blocks, LOSS_THREADS, 0, s>>>(f->views, f->pairs, f->L.num_pairs, f->image, ws, loss_out);
     GS_CUDA_CHECK();
     return GSEVT_OK;
 }

@@ -184,11 +184,13 @@ __device__ inline void write_view_pose(gsevt_view *V, const float *R, const floa
 // in flight, then warp and block combinations in a fixed order.  The pose state is staged in shared memory.  Warp 0 then runs the serial part with its lanes sharing the
 // independent pieces: the two views' chain terms (lanes 0, 1), the four Adam groups
 // (lanes 0-3), the pose update (lane 0) and the two view rewrites (lanes 0, 1).
-__global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, const gsevt_map *maps,
+// threads of the finalize block: half of them reduce each view's twist partials
+#define FIN_THREADS 512
+__global__ void __launch_bounds__(FIN_THREADS) k_track_finalize(gsevt_view *views, const gsevt_map *maps,
                                                              gsevt_pose_state *poses, int num_poses, Workspace ws,
                                                              const double *loss, gsevt_pair *pairs, int num_pairs)
 {
-    __shared__ float2 part[2][GS_BLOCK / 32][6];
+    __shared__ float2 part[2][FIN_THREADS / 32][6];
     __shared__ gsevt_pose_state S;
     __shared__ float s_g[2][6], s_acc[2][12], s_grad[12], s_delta[12];
     __shared__ int s_ok;
@@ -198,13 +200,13 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
     // the iteration's sort gave up: leave the pose state as it is (uniform)
     if (gs_sort_timed_out(ws.status)) return;
     if (poses[pi].control && poses[pi].frozen) return;  // this problem's level is finished (uniform)
-    for (int i = threadIdx.x; i < WORDS; i += GS_BLOCK)
+    for (int i = threadIdx.x; i < WORDS; i += FIN_THREADS)
         ((uint32_t *)&S)[i] = ((const uint32_t *)(poses + pi))[i];
     __syncthreads();
     const int vids[2] = {S.last_view, S.next_view};
     {
         // the two views are reduced concurrently, each by half of the block
-        constexpr int HALF = GS_BLOCK / 2;
+        constexpr int HALF = FIN_THREADS / 2;
         const int k = threadIdx.x / HALF, t = threadIdx.x % HALF;
         const gsevt_view &V = views[vids[k]];
         const int nb = (maps[V.map].n + GS_BLOCK - 1) / GS_BLOCK;
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(GS_BLOCK) k_track_finalize(gsevt_view *views, 
     if (threadIdx.x < 12) {
         const int k = threadIdx.x / 6, q = threadIdx.x % 6;
         FP2 sm;
-        for (int w = 0; w < GS_BLOCK / 64; ++w) sm.add(part[k][w][q].x, part[k][w][q].y);
+        for (int w = 0; w < FIN_THREADS / 64; ++w) sm.add(part[k][w][q].x, part[k][w][q].y);
         const double v = (double)sm.hi + (double)sm.lo;
         ws.xi[6 * vids[k] + q] = v;
         s_g[k][q] = (float)v;
@@ -486,7 +488,7 @@ __global__ void k_view_from_settings(const float *vm_t, const float *pr_t, const
 int gs_launch_track_finalize(const gsevt_frame *f, const Workspace &ws, gsevt_pose_state *poses, int num_poses,
                              const double *loss, cudaStream_t s)
 {
-    k_track_finalize<<<num_poses, GS_BLOCK, 0, s>>>((gsevt_view *)f->views, f->maps, poses, num_poses, ws, loss,
+    k_track_finalize<<<num_poses, FIN_THREADS, 0, s>>>((gsevt_view *)f->views, f->maps, poses, num_poses, ws, loss,
                                                     (gsevt_pair *)f->pairs, f->L.num_pairs);
     GS_CUDA_CHECK();
     return GSEVT_OK;
