@@ -12,7 +12,8 @@
 //
 // Blending (the published 3DGS rule): alpha = min(0.99, o * exp(power)), skipped when
 // power > 0 or alpha < 1/255; C += c alpha T (one fused multiply-add); T *= 1 - alpha.
-// power is gs_power and exp is gs_expf, so the per-pixel decisions and sums are
+// exp(power) is evaluated in base 2 as gs_exp2f(y) with y = gs_power2(K, d) = log2(e) power
+// (K the record's conic scaled by gs_log2_conic), so the per-pixel decisions and sums are
 // bit-identical to the CPU oracle, which uses the same operation order.
 //
 // Adjoint: the same front-to-back traversal with the same decisions (no per-pixel
@@ -97,10 +98,10 @@ template <bool RGB> struct alignas(128) Batch {
 
 // Conservative pixel box of a Gaussian's alpha support.  A pixel blends the Gaussian
 // only if alpha = min(0.99, o exp(power)) >= 1/255, i.e. -power <= tau = ln(255 o).  With
-// M the conic, -power = d^T M d / 2 in exact arithmetic; the FP32 evaluation (gs_power:
+// M the conic, -power = d^T M d / 2 in exact arithmetic; the FP32 evaluation (gs_power2:
 // five products and two fused multiply-adds) deviates by less than 1e-6 tr(M) |d|^2, so
 // every pixel that can pass satisfies Q(d) = d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the
-// slack also covers gs_expf's and logf's rounding).  The box of that ellipse, widened by 0.1 % + 0.5 px,
+// slack also covers gs_exp2f's and logf's rounding).  The box of that ellipse, widened by 0.1 % + 0.5 px,
 // therefore never excludes a pixel whose per-pixel test would pass, so culling against it
 // leaves every blending decision - and the result bits - unchanged.
 // Also returns, through *ell, Q's coefficients {a, b, c} (Q = a dx^2 + 2 b dx dy + c dy^2;
@@ -288,7 +289,7 @@ __device__ __forceinline__ void warp_pixel(int tid, int tx, int ty, int &px, int
 
 // One candidate of the forward blend for one lane.  Every lane evaluates it and the
 // decisions are predicates (selects instead of divergent branches; stopped lanes change
-// nothing).  A candidate is skipped when power > 0 or alpha < 1/255; the pixel stops
+// nothing).  A candidate is skipped when y > 0 or alpha < 1/255; the pixel stops
 // before a candidate that would take T below 1e-4.
 template <bool EXTRAS, bool RGB>
 __device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const BlendParams &p, int j, int r, float pxf,
@@ -297,10 +298,10 @@ __device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const Blend
 {
     const float4 A = cur.r[j].A, B = cur.r[j].B;
     const float dx = A.x - pxf, dy = A.y - pyf;
-    const float power = gs_power(B.x, B.y, B.z, dx, dy);
-    const float alpha = fminf(0.99f, B.w * gs_expf(power));
+    const float y = gs_power2(gs_log2_conic(B), dx, dy);
+    const float alpha = fminf(0.99f, B.w * gs_exp2f(y));
     const float test_T = T * (1.0f - alpha);
-    const bool pass = !done && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
+    const bool pass = !done && !(y > 0.0f) && !(alpha < 1.0f / 255.0f);
     const bool stop = pass && test_T < 0.0001f;
     const bool use = pass && !stop;
     done = done || stop;
@@ -536,16 +537,17 @@ __device__ __forceinline__ float pair_pixel_grad(const BlendParams &p, const gse
 // One candidate of the tracker adjoint (grey, pair-loss gradient gC per pixel): the
 // forward's decisions as predicates, the state update, and the six terms (the five
 // power-gradient moments and the colour gradient), zero for a lane that does not blend it.
-__device__ __forceinline__ bool tracker_candidate(const Rec *rec, int j, float pxf, float pyf, float Cimg, float gC,
-                                                  float &T, float &Pc, bool &done, float (&g)[6])
+// A: the record's {mean x, mean y, depth, grey}; K: its base-2 conic and opacity.
+__device__ __forceinline__ bool tracker_candidate(const float4 A, const float4 K, float pxf, float pyf, float Cimg,
+                                                  float gC, float &T, float &Pc, bool &done, float (&g)[6])
 {
-    const float4 A = rec[j].A, B = rec[j].B;
     const float dx = A.x - pxf, dy = A.y - pyf;
-    const float power = gs_power(B.x, B.y, B.z, dx, dy);
-    const float araw = B.w * gs_expf(power);
+    const float y = gs_power2(K, dx, dy);
+    // araw = o exp(power), whose derivative in the (natural) power is araw itself
+    const float araw = K.w * gs_exp2f(y);
     const float alpha = fminf(0.99f, araw);
     const float test_T = T * (1.0f - alpha);
-    const bool pass = !done && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
+    const bool pass = !done && !(y > 0.0f) && !(alpha < 1.0f / 255.0f);
     const bool stop = pass && test_T < 0.0001f;
     const bool contrib = pass && !stop;
     done = done || stop;
@@ -694,9 +696,12 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
                     const int jb = has_b ? c0 + __ffs(mask) - 1 : ja;
                     if (has_b) mask &= mask - 1;
                     float ga[6], gb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-                    const bool ca = tracker_candidate(cur.r, ja, pxf, pyf, Cimg[0], gC[0], T, Pc[0], done, ga);
+                    const bool ca = tracker_candidate(cur.r[ja].A, gs_log2_conic(cur.r[ja].B), pxf, pyf, Cimg[0],
+                                                      gC[0], T, Pc[0], done, ga);
                     bool cb = false;
-                    if (has_b) cb = tracker_candidate(cur.r, jb, pxf, pyf, Cimg[0], gC[0], T, Pc[0], done, gb);
+                    if (has_b)
+                        cb = tracker_candidate(cur.r[jb].A, gs_log2_conic(cur.r[jb].B), pxf, pyf, Cimg[0], gC[0], T,
+                                               Pc[0], done, gb);
                     if (__any_sync(0xffffffffu, ca || cb)) {
                         const float s = warp_reduce_pair6(ga, gb, lane);
                         const int q = (lane >> 1) & 7;
@@ -714,12 +719,12 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
                 // a lane that does not blend it contributes zeros and keeps its state).
                 const float4 A = cur.r[j].A, B = cur.r[j].B;
                 const float dx = A.x - pxf, dy = A.y - pyf;
-                const float power = gs_power(B.x, B.y, B.z, dx, dy);
-                const float G = gs_expf(power);
+                const float y = gs_power2(gs_log2_conic(B), dx, dy);
+                const float G = gs_exp2f(y);
                 const float araw = B.w * G;
                 const float alpha = fminf(0.99f, araw);
                 const float test_T = T * (1.0f - alpha);
-                const bool pass = !done && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
+                const bool pass = !done && !(y > 0.0f) && !(alpha < 1.0f / 255.0f);
                 const bool stop = pass && test_T < 0.0001f;
                 const bool contrib = pass && !stop;
                 done = done || stop;
@@ -857,6 +862,7 @@ __global__ void __launch_bounds__(GS_BLOCK, MODE == 0 ? 5 : 1) k_blend_bwd(Blend
 
 struct alignas(128) Batch2 {
     Rec r[PX2_THREADS];
+    float4 k[PX2_THREADS];  // the base-2 conic and opacity of each record (gs_log2_conic)
     float4 box[PX2_THREADS];
     float4 ell[PX2_THREADS];
     uint32_t id[PX2_THREADS];
@@ -876,15 +882,14 @@ __device__ __forceinline__ void load_batch2(const BlendParams &p, Batch2 &buf, u
 
 // One candidate of the grey forward blend (no extras) for one pixel: the arithmetic of
 // fwd_candidate<false, false>, so the image bits are the same.
-__device__ __forceinline__ void grey_candidate(const Rec *rec, int j, float pxf, float pyf, float &T, float &C,
-                                               bool &done)
+__device__ __forceinline__ void grey_candidate(const float4 A, const float4 K, float pxf, float pyf, float &T,
+                                               float &C, bool &done)
 {
-    const float4 A = rec[j].A, B = rec[j].B;
     const float dx = A.x - pxf, dy = A.y - pyf;
-    const float power = gs_power(B.x, B.y, B.z, dx, dy);
-    const float alpha = fminf(0.99f, B.w * gs_expf(power));
+    const float y = gs_power2(K, dx, dy);
+    const float alpha = fminf(0.99f, K.w * gs_exp2f(y));
     const float test_T = T * (1.0f - alpha);
-    const bool pass = !done && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
+    const bool pass = !done && !(y > 0.0f) && !(alpha < 1.0f / 255.0f);
     const bool stop = pass && test_T < 0.0001f;
     const bool use = pass && !stop;
     done = done || stop;
@@ -930,8 +935,10 @@ __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_fwd_px2(BlendParams p)
         const int n = min(PX2_THREADS, todo - r * PX2_THREADS);
         if ((int)threadIdx.x < n) {
             float4 e;
-            cur.box[threadIdx.x] = gauss_box(cur.r[threadIdx.x].A, cur.r[threadIdx.x].B, &e);
+            const float4 B = cur.r[threadIdx.x].B;
+            cur.box[threadIdx.x] = gauss_box(cur.r[threadIdx.x].A, B, &e);
             cur.ell[threadIdx.x] = e;
+            cur.k[threadIdx.x] = gs_log2_conic(B);
         }
         __syncthreads();
         bool warp_done = false;
@@ -943,13 +950,15 @@ __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_fwd_px2(BlendParams p)
                 if (__all_sync(0xffffffffu, d0 && d1)) { warp_done = true; break; }
                 const int ja = c0 + __ffs(mask) - 1;
                 mask &= mask - 1;
-                grey_candidate(cur.r, ja, pxf, py0f, T0, C0, d0);
-                grey_candidate(cur.r, ja, pxf, py1f, T1, C1, d1);
+                const float4 Aa = cur.r[ja].A, Ka = cur.k[ja];
+                grey_candidate(Aa, Ka, pxf, py0f, T0, C0, d0);
+                grey_candidate(Aa, Ka, pxf, py1f, T1, C1, d1);
                 if (mask) {
                     const int jb = c0 + __ffs(mask) - 1;
                     mask &= mask - 1;
-                    grey_candidate(cur.r, jb, pxf, py0f, T0, C0, d0);
-                    grey_candidate(cur.r, jb, pxf, py1f, T1, C1, d1);
+                    const float4 Ab = cur.r[jb].A, Kb = cur.k[jb];
+                    grey_candidate(Ab, Kb, pxf, py0f, T0, C0, d0);
+                    grey_candidate(Ab, Kb, pxf, py1f, T1, C1, d1);
                 }
             }
         }
@@ -1015,8 +1024,10 @@ __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_bwd_px2(BlendParams p)
         const int n = min(PX2_THREADS, todo - r * PX2_THREADS);
         if ((int)threadIdx.x < n) {
             float4 e;
-            cur.box[threadIdx.x] = gauss_box(cur.r[threadIdx.x].A, cur.r[threadIdx.x].B, &e);
+            const float4 B = cur.r[threadIdx.x].B;
+            cur.box[threadIdx.x] = gauss_box(cur.r[threadIdx.x].A, B, &e);
             cur.ell[threadIdx.x] = e;
+            cur.k[threadIdx.x] = gs_log2_conic(B);
         }
         __syncthreads();
         bool warp_done = false;
@@ -1031,14 +1042,16 @@ __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_bwd_px2(BlendParams p)
                 const int jb = has_b ? c0 + __ffs(mask) - 1 : ja;
                 if (has_b) mask &= mask - 1;
                 float ga[6], gb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, h[6];
-                const bool ca0 = tracker_candidate(cur.r, ja, pxf, py0f, Cimg0, gC0, T0, P0, d0, ga);
-                const bool ca1 = tracker_candidate(cur.r, ja, pxf, py1f, Cimg1, gC1, T1, P1, d1, h);
+                const float4 Aa = cur.r[ja].A, Ka = cur.k[ja];
+                const bool ca0 = tracker_candidate(Aa, Ka, pxf, py0f, Cimg0, gC0, T0, P0, d0, ga);
+                const bool ca1 = tracker_candidate(Aa, Ka, pxf, py1f, Cimg1, gC1, T1, P1, d1, h);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) ga[k] += h[k];
                 bool cb = false;
                 if (has_b) {
-                    const bool cb0 = tracker_candidate(cur.r, jb, pxf, py0f, Cimg0, gC0, T0, P0, d0, gb);
-                    const bool cb1 = tracker_candidate(cur.r, jb, pxf, py1f, Cimg1, gC1, T1, P1, d1, h);
+                    const float4 Ab = cur.r[jb].A, Kb = cur.k[jb];
+                    const bool cb0 = tracker_candidate(Ab, Kb, pxf, py0f, Cimg0, gC0, T0, P0, d0, gb);
+                    const bool cb1 = tracker_candidate(Ab, Kb, pxf, py1f, Cimg1, gC1, T1, P1, d1, h);
 #pragma unroll
                     for (int k = 0; k < 6; ++k) gb[k] += h[k];
                     cb = cb0 || cb1;

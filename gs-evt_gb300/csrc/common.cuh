@@ -32,42 +32,53 @@
 #define GS_COOP_GP 160
 
 // ----------------------------------------------------------------- exp ----------
-// Deterministic exp for x <= 0: Cody & Waite (1980) reduction x = k ln2 + r with a
-// two-part ln2, e^r = 1 + r + r^2 q(r) with q a degree-4 near-minimax polynomial (Lawson
-// fit, oracle/fit_exp.py; Horner with fused multiply-adds) and an exact power-of-two
-// scale: below 0.88 ulp.  Bit-identical to or_expf in the CPU oracle.  Returns 0 for
-// x < -87 and for NaN.
-__host__ __device__ __forceinline__ float gs_expf(float x)
+// The blends evaluate a Gaussian's weight in base 2: with the conic (cx, cy, cz) scaled
+// once per record to K = (-log2(e)/2 cx, -log2(e) cy, -log2(e)/2 cz), the exponent
+// y = Kx dx^2 + Ky dx dy + Kz dy^2 is log2(e) times the published power
+// -(cx dx^2 + cz dy^2)/2 - cy dx dy, and the weight is 2^y.  The FP32 operation order (three
+// products for K, then gs_power2) is the CPU oracle's, so every decision and image bit is
+// shared with it.
+#define GS_KHALF (-0x1.715476p-1f)  // -log2(e) / 2, rounded to FP32
+#define GS_KFULL (-0x1.715476p+0f)  // -log2(e)
+
+// Deterministic 2^y for y <= 0: k = rint(y), r = y - k (exact, |r| <= 1/2), 2^r = 1 + r c(r)
+// with c a degree-5 near-minimax polynomial (Lawson fit, oracle/fit_exp.py fit_exp2;
+// Horner with fused multiply-adds) and an exact power-of-two scale: below one ulp of 2^y.
+// Bit-identical to or_exp2f in the CPU oracle.  Returns 0 for y < -126 and for NaN.
+__host__ __device__ __forceinline__ float gs_exp2f(float y)
 {
-    if (!(x >= -87.0f)) return 0.0f;
-    float k = rintf(x * 0x1.715476p+0f);
-    float r = fmaf(k, -0x1.62e4p-1f, x);
-    r = fmaf(k, -0x1.7f7d1cp-20f, r);
-    float p = 0x1.6a2444p-10f;
-    p = fmaf(p, r, 0x1.1239d6p-7f);
-    p = fmaf(p, r, 0x1.5558f2p-5f);
-    p = fmaf(p, r, 0x1.555492p-3f);
-    p = fmaf(p, r, 0x1.fffffcp-2f);
+    if (!(y >= -126.0f)) return 0.0f;
+    const float k = rintf(y);
+    const float r = y - k;
+    float p = 0x1.41fbb8p-13f;
+    p = fmaf(p, r, 0x1.5f3e56p-10f);
+    p = fmaf(p, r, 0x1.3b2d4ep-7f);
+    p = fmaf(p, r, 0x1.c6aee8p-5f);
+    p = fmaf(p, r, 0x1.ebfbdcp-3f);
+    p = fmaf(p, r, 0x1.62e43p-1f);
     p = fmaf(p, r, 1.0f);
-    p = fmaf(p, r, 1.0f);
-    int ki = (int)k;
+    const int ki = (int)k;
 #ifdef __CUDA_ARCH__
-    float sc = __int_as_float((ki + 127) << 23);
+    const float sc = __int_as_float((ki + 127) << 23);
 #else
     union { uint32_t u; float f; } cv;
     cv.u = (uint32_t)(ki + 127) << 23;
-    float sc = cv.f;
+    const float sc = cv.f;
 #endif
     return p * sc;
 }
 
-// Exponent of a Gaussian at pixel offset d = mean - pixel, -(cx dx^2 + cz dy^2) / 2 - cy dx dy
-// for the conic (cx, cy, cz), in a fixed FP32 operation order (the CPU oracle's blend uses
-// the same one): the two squares are summed with one fused multiply-add.
-__host__ __device__ __forceinline__ float gs_power(float cx, float cy, float cz, float dx, float dy)
+// The base-2 exponent coefficients of a record's conic {cx, cy, cz, opacity} (opacity kept).
+__host__ __device__ __forceinline__ float4 gs_log2_conic(float4 B)
 {
-    const float q = fmaf(cz * dy, dy, (cx * dx) * dx);
-    return fmaf(-0.5f, q, -((cy * dx) * dy));
+    return make_float4(GS_KHALF * B.x, GS_KFULL * B.y, GS_KHALF * B.z, B.w);
+}
+
+// The base-2 exponent at pixel offset d = mean - pixel: Kx dx^2 + Kz dy^2 + Ky dx dy, the
+// first two summed with one fused multiply-add and the cross term added with another.
+__host__ __device__ __forceinline__ float gs_power2(float4 K, float dx, float dy)
+{
+    return fmaf(K.y * dx, dy, fmaf(K.z * dy, dy, (K.x * dx) * dx));
 }
 
 // ------------------------------------------------------------ workspace ---------

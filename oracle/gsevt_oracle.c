@@ -36,25 +36,26 @@
 #define TILE 16
 
 /* ---------------------------------------------------------------- exp -------- */
-/* Deterministic exp for x <= 0 used by the blending stages on both CPU and GPU.
- * Method: Cody & Waite (1980) argument reduction x = k ln2 + r with ln2 split into a
- * short high part (exact products k*LN2_HI for |k| < 2^9) and a low correction, then
- * e^r = 1 + r + r^2 q(r) on |r| <= ln2/2 with q a degree-4 near-minimax polynomial
- * (Lawson's reweighted least squares, oracle/fit_exp.py) evaluated with fused
- * multiply-adds, and an exact power-of-two scale.  Max error < 0.88 ulp (checked
- * against numpy in tests/test_oracle.py).  Returns 0 for x < -87 and NaN. */
-static float or_expf(float x)
+/* The blend's weight in base 2 (the CUDA blends' gs_log2_conic / gs_power2 / gs_exp2f):
+ * the conic (cx, cy, cz) scaled to K = (-log2(e)/2 cx, -log2(e) cy, -log2(e)/2 cz), the
+ * exponent y = Kx dx^2 + Ky dx dy + Kz dy^2 (log2(e) times the published power) and the
+ * weight 2^y.  Deterministic 2^y for y <= 0: k = rint(y), r = y - k exact, 2^r = 1 + r c(r)
+ * with c of degree 5 (Lawson's reweighted least squares, oracle/fit_exp.py fit_exp2)
+ * evaluated with fused multiply-adds, and an exact power-of-two scale.  Max error below one
+ * ulp (checked against numpy in tests/test_oracle.py).  Returns 0 for y < -126 and NaN. */
+#define OR_KHALF (-0x1.715476p-1f)
+#define OR_KFULL (-0x1.715476p+0f)
+static float or_exp2f(float y)
 {
-    if (!(x >= -87.0f)) return 0.0f;
-    float k = rintf(x * 0x1.715476p+0f);
-    float r = fmaf(k, -0x1.62e4p-1f, x);
-    r = fmaf(k, -0x1.7f7d1cp-20f, r);
-    float p = 0x1.6a2444p-10f;
-    p = fmaf(p, r, 0x1.1239d6p-7f);
-    p = fmaf(p, r, 0x1.5558f2p-5f);
-    p = fmaf(p, r, 0x1.555492p-3f);
-    p = fmaf(p, r, 0x1.fffffcp-2f);
-    p = fmaf(p, r, 1.0f);
+    if (!(y >= -126.0f)) return 0.0f;
+    float k = rintf(y);
+    float r = y - k;
+    float p = 0x1.41fbb8p-13f;
+    p = fmaf(p, r, 0x1.5f3e56p-10f);
+    p = fmaf(p, r, 0x1.3b2d4ep-7f);
+    p = fmaf(p, r, 0x1.c6aee8p-5f);
+    p = fmaf(p, r, 0x1.ebfbdcp-3f);
+    p = fmaf(p, r, 0x1.62e43p-1f);
     p = fmaf(p, r, 1.0f);
     int ki = (int)k;
     uint32_t bits = (uint32_t)(ki + 127) << 23;
@@ -63,7 +64,7 @@ static float or_expf(float x)
     return p * sc;
 }
 
-float or_expf_export(float x) { return or_expf(x); }
+float or_exp2f_export(float y) { return or_exp2f(y); }
 
 /* ------------------------------------------------------- FP32 / FP64 instances */
 #define REAL float
@@ -246,13 +247,14 @@ void or_blend_fwd(int W, int H, int nch, const uint32_t *ranges, const uint32_t 
                 for (uint32_t j = s; j < e; ++j) {
                     uint32_t g = vals[j];
                     float dx = mean2d[2 * g] - pxf, dy = mean2d[2 * g + 1] - pyf;
-                    float cx = conic[3 * g], cy = conic[3 * g + 1], cz = conic[3 * g + 2];
-                    /* the two squares summed with one fused multiply-add (the CUDA blend's
-                     * gs_power uses the same order) */
-                    float q = fmaf(cz * dy, dy, (cx * dx) * dx);
-                    float power = fmaf(-0.5f, q, -((cy * dx) * dy));
-                    if (power > 0.0f) continue;
-                    float G = or_expf(power);
+                    /* base-2 exponent: K from the conic, then the two squares summed with
+                     * one fused multiply-add and the cross term with another (the CUDA
+                     * blends' gs_log2_conic and gs_power2 use the same order) */
+                    float kx = OR_KHALF * conic[3 * g], ky = OR_KFULL * conic[3 * g + 1];
+                    float kz = OR_KHALF * conic[3 * g + 2];
+                    float y2 = fmaf(ky * dx, dy, fmaf(kz * dy, dy, (kx * dx) * dx));
+                    if (y2 > 0.0f) continue;
+                    float G = or_exp2f(y2);
                     float araw = opac[g] * G;
                     float alpha = fminf(0.99f, araw);
                     if (alpha < 1.0f / 255.0f) continue;

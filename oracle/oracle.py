@@ -41,8 +41,8 @@ def lib():
     if _lib is None:
         path = build_oracle.build()
         L = C.CDLL(path)
-        L.or_expf_export.restype = C.c_float
-        L.or_expf_export.argtypes = [C.c_float]
+        L.or_exp2f_export.restype = C.c_float
+        L.or_exp2f_export.argtypes = [C.c_float]
         L.or_cov3d.argtypes = [C.c_int, f32p, f32p, C.c_float, f32p]
         L.or_sh_eval_f64.argtypes = [C.c_int, C.c_int, f32p, f64p, f64p]
         L.or_preprocess.argtypes = [C.c_int, f32p, f32p, _opt(f32p), C.c_int, _opt(f32p), f32p,
@@ -82,8 +82,8 @@ def _c(a, dt):
     return None if a is None else np.ascontiguousarray(a, dtype=dt)
 
 
-def expf(x):
-    return np.float32(lib().or_expf_export(float(x)))
+def exp2f(y):
+    return np.float32(lib().or_exp2f_export(float(y)))
 
 
 def cov3d(scale, rot, mod=1.0):

@@ -18,14 +18,16 @@ GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_gold
 
 
 # ----------------------------------------------------------------------- exp --
-def test_expf_error_bound():
-    xs = np.linspace(-87.0, 0.0, 20001).astype(np.float32)
-    xs = np.concatenate([xs, np.float32([-5.6, -5.55, -1e-7, -0.0, -0.3465736, -0.6931472])])
-    got = np.array([oracle.expf(x) for x in xs], np.float64)
-    ref = np.exp(xs.astype(np.float64))
+def test_exp2f_error_bound():
+    ys = np.linspace(-126.0, 0.0, 40001).astype(np.float32)
+    ys = np.concatenate([ys, np.float32([-8.0, -8.5, -7.5, -1e-7, -0.0, -0.5, -1.5, -0.4999999, -125.9])])
+    got = np.array([oracle.exp2f(y) for y in ys], np.float64)
+    ref = np.exp2(ys.astype(np.float64))
     ulp = np.abs(got - ref) / np.spacing(np.float32(ref).astype(np.float32)).astype(np.float64)
     assert ulp.max() <= 1.0, ulp.max()
-    assert oracle.expf(-88.0) == 0.0 and oracle.expf(float("nan")) == 0.0
+    assert oracle.exp2f(-126.5) == 0.0 and oracle.exp2f(float("nan")) == 0.0
+    # integers are exact
+    assert all(oracle.exp2f(float(-k)) == np.float32(2.0 ** -k) for k in range(0, 126))
 
 
 # ------------------------------------------------------------- pose golden --
