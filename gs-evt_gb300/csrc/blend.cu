@@ -99,7 +99,8 @@ template <bool RGB> struct alignas(128) Batch {
 // Conservative pixel box of a Gaussian's alpha support.  A pixel blends the Gaussian
 // only if alpha = min(0.99, o exp(power)) >= 1/255, i.e. -power <= tau = ln(255 o).  With
 // M the conic, -power = d^T M d / 2 in exact arithmetic; the FP32 evaluation (gs_power2:
-// five products and two fused multiply-adds) deviates by less than 1e-6 tr(M) |d|^2, so
+// three products for K, three in the exponent and two fused multiply-adds) deviates by
+// less than 1e-6 tr(M) |d|^2, so
 // every pixel that can pass satisfies Q(d) = d^T (M/2 - 1e-6 tr(M) I) d <= tau + 1e-4 (the
 // slack also covers gs_exp2f's and logf's rounding).  The box of that ellipse, widened by 0.1 % + 0.5 px,
 // therefore never excludes a pixel whose per-pixel test would pass, so culling against it
@@ -300,7 +301,7 @@ __device__ __forceinline__ void fwd_candidate(const Batch<RGB> &cur, const Blend
     const float dx = A.x - pxf, dy = A.y - pyf;
     const float y = gs_power2(gs_log2_conic(B), dx, dy);
     const float alpha = fminf(0.99f, B.w * gs_exp2f(y));
-    const float test_T = T * (1.0f - alpha);
+    const float test_T = fmaf(-T, alpha, T);  // T (1 - alpha), one rounding
     const bool pass = !done && !(y > 0.0f) && !(alpha < 1.0f / 255.0f);
     const bool stop = pass && test_T < 0.0001f;
     const bool use = pass && !stop;
@@ -546,7 +547,7 @@ __device__ __forceinline__ bool tracker_candidate(const float4 A, const float4 K
     // araw = o exp(power), whose derivative in the (natural) power is araw itself
     const float araw = K.w * gs_exp2f(y);
     const float alpha = fminf(0.99f, araw);
-    const float test_T = T * (1.0f - alpha);
+    const float test_T = fmaf(-T, alpha, T);  // T (1 - alpha), one rounding
     const bool pass = !done && !(y > 0.0f) && !(alpha < 1.0f / 255.0f);
     const bool stop = pass && test_T < 0.0001f;
     const bool contrib = pass && !stop;
@@ -723,7 +724,7 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
                 const float G = gs_exp2f(y);
                 const float araw = B.w * G;
                 const float alpha = fminf(0.99f, araw);
-                const float test_T = T * (1.0f - alpha);
+                const float test_T = fmaf(-T, alpha, T);  // T (1 - alpha), one rounding
                 const bool pass = !done && !(y > 0.0f) && !(alpha < 1.0f / 255.0f);
                 const bool stop = pass && test_T < 0.0001f;
                 const bool contrib = pass && !stop;
@@ -888,7 +889,7 @@ __device__ __forceinline__ void grey_candidate(const float4 A, const float4 K, f
     const float dx = A.x - pxf, dy = A.y - pyf;
     const float y = gs_power2(K, dx, dy);
     const float alpha = fminf(0.99f, K.w * gs_exp2f(y));
-    const float test_T = T * (1.0f - alpha);
+    const float test_T = fmaf(-T, alpha, T);  // T (1 - alpha), one rounding
     const bool pass = !done && !(y > 0.0f) && !(alpha < 1.0f / 255.0f);
     const bool stop = pass && test_T < 0.0001f;
     const bool use = pass && !stop;

@@ -37,7 +37,8 @@
 // y = Kx dx^2 + Ky dx dy + Kz dy^2 is log2(e) times the published power
 // -(cx dx^2 + cz dy^2)/2 - cy dx dy, and the weight is 2^y.  The FP32 operation order (three
 // products for K, then gs_power2) is the CPU oracle's, so every decision and image bit is
-// shared with it.
+// shared with it; so is the transmittance update T (1 - alpha), one fused multiply-add
+// fmaf(-T, alpha, T) in the blends and the oracle.
 #define GS_KHALF (-0x1.715476p-1f)  // -log2(e) / 2, rounded to FP32
 #define GS_KFULL (-0x1.715476p+0f)  // -log2(e)
 
@@ -74,11 +75,11 @@ __host__ __device__ __forceinline__ float4 gs_log2_conic(float4 B)
     return make_float4(GS_KHALF * B.x, GS_KFULL * B.y, GS_KHALF * B.z, B.w);
 }
 
-// The base-2 exponent at pixel offset d = mean - pixel: Kx dx^2 + Kz dy^2 + Ky dx dy, the
-// first two summed with one fused multiply-add and the cross term added with another.
+// The base-2 exponent at pixel offset d = mean - pixel, dx (Kx dx + Ky dy) + Kz dy^2: two
+// fused multiply-adds and three products (Kx dx is shared by the pixels of one column).
 __host__ __device__ __forceinline__ float gs_power2(float4 K, float dx, float dy)
 {
-    return fmaf(K.y * dx, dy, fmaf(K.z * dy, dy, (K.x * dx) * dx));
+    return fmaf(fmaf(K.y, dy, K.x * dx), dx, (K.z * dy) * dy);
 }
 
 // ------------------------------------------------------------ workspace ---------

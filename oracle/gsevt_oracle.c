@@ -247,18 +247,18 @@ void or_blend_fwd(int W, int H, int nch, const uint32_t *ranges, const uint32_t 
                 for (uint32_t j = s; j < e; ++j) {
                     uint32_t g = vals[j];
                     float dx = mean2d[2 * g] - pxf, dy = mean2d[2 * g + 1] - pyf;
-                    /* base-2 exponent: K from the conic, then the two squares summed with
-                     * one fused multiply-add and the cross term with another (the CUDA
-                     * blends' gs_log2_conic and gs_power2 use the same order) */
+                    /* base-2 exponent: K from the conic, then dx (Kx dx + Ky dy) + Kz dy^2
+                     * with two fused multiply-adds (the CUDA blends' gs_log2_conic and
+                     * gs_power2 use the same order) */
                     float kx = OR_KHALF * conic[3 * g], ky = OR_KFULL * conic[3 * g + 1];
                     float kz = OR_KHALF * conic[3 * g + 2];
-                    float y2 = fmaf(ky * dx, dy, fmaf(kz * dy, dy, (kx * dx) * dx));
+                    float y2 = fmaf(fmaf(ky, dy, kx * dx), dx, (kz * dy) * dy);
                     if (y2 > 0.0f) continue;
                     float G = or_exp2f(y2);
                     float araw = opac[g] * G;
                     float alpha = fminf(0.99f, araw);
                     if (alpha < 1.0f / 255.0f) continue;
-                    float test_T = T * (1.0f - alpha);
+                    float test_T = fmaf(-T, alpha, T); /* T (1 - alpha), one rounding */
                     if (test_T < 0.0001f) break;
                     for (int ch = 0; ch < nch; ++ch)
                         C[ch] = fmaf(colors[nch * g + ch] * alpha, T, C[ch]);
