@@ -539,8 +539,10 @@ __device__ __forceinline__ float pair_pixel_grad(const BlendParams &p, const gse
 // forward's decisions as predicates, the state update, and the six terms (the five
 // power-gradient moments and the colour gradient), zero for a lane that does not blend it.
 // A: the record's {mean x, mean y, depth, grey}; K: its base-2 conic and opacity.
-__device__ __forceinline__ bool tracker_candidate(const float4 A, const float4 K, float pxf, float pyf, float Cimg,
-                                                  float gC, float &T, float &Pc, bool &done, float (&g)[6])
+// S: the colour behind this candidate so far, the rendered pixel minus the front-to-back
+// sum of the candidates blended before it (it starts at the pixel's value).
+__device__ __forceinline__ bool tracker_candidate(const float4 A, const float4 K, float pxf, float pyf, float gC,
+                                                  float &T, float &S, bool &done, float (&g)[6])
 {
     const float dx = A.x - pxf, dy = A.y - pyf;
     const float y = gs_power2(K, dx, dy);
@@ -555,8 +557,8 @@ __device__ __forceinline__ bool tracker_candidate(const float4 A, const float4 K
     const float wgt = contrib ? alpha * T : 0.0f;
     // gradient-only term: the 2-ulp fast reciprocal suffices
     const float inv1m = __fdividef(1.0f, 1.0f - alpha);
-    Pc = contrib ? __fmaf_rn(A.w, wgt, Pc) : Pc;
-    const float dal = gC * __fmaf_rn(-(Cimg - Pc), inv1m, T * A.w);
+    S = contrib ? __fmaf_rn(-A.w, wgt, S) : S;
+    const float dal = gC * __fmaf_rn(-S, inv1m, T * A.w);
     // below the 0.99 clamp alpha depends on the power
     const float dpow = (contrib && araw <= 0.99f) ? dal * araw : 0.0f;
     const float mx = dpow * dx, my = dpow * dy;
@@ -647,6 +649,7 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
     }
 
     float T = 1.0f, Pc[3] = {0, 0, 0}, PD = 0.0f, PA = 0.0f;
+    if (MODE == 0) Pc[0] = Cimg[0];  // the tracker adjoint tracks the suffix instead of the prefix
     bool done = !inside;
     int issued = 0, waited = 0;  // TMA: batches issued / waited for
     if (rounds > 0) {
@@ -697,12 +700,13 @@ __device__ __forceinline__ void bwd_tile(const BlendParams &p, const CUtensorMap
                     const int jb = has_b ? c0 + __ffs(mask) - 1 : ja;
                     if (has_b) mask &= mask - 1;
                     float ga[6], gb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-                    const bool ca = tracker_candidate(cur.r[ja].A, gs_log2_conic(cur.r[ja].B), pxf, pyf, Cimg[0],
-                                                      gC[0], T, Pc[0], done, ga);
+                    // Pc[0] holds the suffix (the pixel minus the blended prefix) here
+                    const bool ca = tracker_candidate(cur.r[ja].A, gs_log2_conic(cur.r[ja].B), pxf, pyf, gC[0], T,
+                                                      Pc[0], done, ga);
                     bool cb = false;
                     if (has_b)
-                        cb = tracker_candidate(cur.r[jb].A, gs_log2_conic(cur.r[jb].B), pxf, pyf, Cimg[0], gC[0], T,
-                                               Pc[0], done, gb);
+                        cb = tracker_candidate(cur.r[jb].A, gs_log2_conic(cur.r[jb].B), pxf, pyf, gC[0], T, Pc[0],
+                                               done, gb);
                     if (__any_sync(0xffffffffu, ca || cb)) {
                         const float s = warp_reduce_pair6(ga, gb, lane);
                         const int q = (lane >> 1) & 7;
@@ -1010,7 +1014,7 @@ __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_bwd_px2(BlendParams p)
     const uint2 range = p.ws.ranges[tile];
     const int todo = (int)(range.y - range.x);
     const int rounds = (todo + PX2_THREADS - 1) / PX2_THREADS;
-    float T0 = 1.0f, T1 = 1.0f, P0 = 0.0f, P1 = 0.0f;
+    float T0 = 1.0f, T1 = 1.0f, S0 = Cimg0, S1 = Cimg1;  // transmittance and suffix per pixel
     bool d0 = !in0, d1 = !in1;
     if (rounds > 0) load_batch2(p, sb[0], range, 0);
     for (int r = 0; r < rounds; ++r) {
@@ -1044,15 +1048,15 @@ __global__ void __launch_bounds__(PX2_THREADS, 8) k_blend_bwd_px2(BlendParams p)
                 if (has_b) mask &= mask - 1;
                 float ga[6], gb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, h[6];
                 const float4 Aa = cur.r[ja].A, Ka = cur.k[ja];
-                const bool ca0 = tracker_candidate(Aa, Ka, pxf, py0f, Cimg0, gC0, T0, P0, d0, ga);
-                const bool ca1 = tracker_candidate(Aa, Ka, pxf, py1f, Cimg1, gC1, T1, P1, d1, h);
+                const bool ca0 = tracker_candidate(Aa, Ka, pxf, py0f, gC0, T0, S0, d0, ga);
+                const bool ca1 = tracker_candidate(Aa, Ka, pxf, py1f, gC1, T1, S1, d1, h);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) ga[k] += h[k];
                 bool cb = false;
                 if (has_b) {
                     const float4 Ab = cur.r[jb].A, Kb = cur.k[jb];
-                    const bool cb0 = tracker_candidate(Ab, Kb, pxf, py0f, Cimg0, gC0, T0, P0, d0, gb);
-                    const bool cb1 = tracker_candidate(Ab, Kb, pxf, py1f, Cimg1, gC1, T1, P1, d1, h);
+                    const bool cb0 = tracker_candidate(Ab, Kb, pxf, py0f, gC0, T0, S0, d0, gb);
+                    const bool cb1 = tracker_candidate(Ab, Kb, pxf, py1f, gC1, T1, S1, d1, h);
 #pragma unroll
                     for (int k = 0; k < 6; ++k) gb[k] += h[k];
                     cb = cb0 || cb1;

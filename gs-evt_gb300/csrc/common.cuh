@@ -45,10 +45,12 @@
 // Deterministic 2^y for y <= 0: k = rint(y), r = y - k (exact, |r| <= 1/2), 2^r = 1 + r c(r)
 // with c a degree-5 near-minimax polynomial (Lawson fit, oracle/fit_exp.py fit_exp2;
 // Horner with fused multiply-adds) and an exact power-of-two scale: below one ulp of 2^y.
-// Bit-identical to or_exp2f in the CPU oracle.  Returns 0 for y < -126 and for NaN.
+// Bit-identical to or_exp2f in the CPU oracle.  y below -126 (and NaN) is raised to -126:
+// a weight of 2^-126 fails the blends' alpha test exactly as 0 would, one instruction
+// cheaper than a branch.
 __host__ __device__ __forceinline__ float gs_exp2f(float y)
 {
-    if (!(y >= -126.0f)) return 0.0f;
+    y = fmaxf(y, -126.0f);
     const float k = rintf(y);
     const float r = y - k;
     float p = 0x1.41fbb8p-13f;

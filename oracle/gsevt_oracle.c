@@ -42,12 +42,13 @@
  * weight 2^y.  Deterministic 2^y for y <= 0: k = rint(y), r = y - k exact, 2^r = 1 + r c(r)
  * with c of degree 5 (Lawson's reweighted least squares, oracle/fit_exp.py fit_exp2)
  * evaluated with fused multiply-adds, and an exact power-of-two scale.  Max error below one
- * ulp (checked against numpy in tests/test_oracle.py).  Returns 0 for y < -126 and NaN. */
+ * ulp (checked against numpy in tests/test_oracle.py).  y below -126 and NaN are raised to
+ * -126 (2^-126 fails the alpha test as 0 would). */
 #define OR_KHALF (-0x1.715476p-1f)
 #define OR_KFULL (-0x1.715476p+0f)
 static float or_exp2f(float y)
 {
-    if (!(y >= -126.0f)) return 0.0f;
+    y = fmaxf(y, -126.0f);
     float k = rintf(y);
     float r = y - k;
     float p = 0x1.41fbb8p-13f;

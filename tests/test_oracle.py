@@ -25,7 +25,9 @@ def test_exp2f_error_bound():
     ref = np.exp2(ys.astype(np.float64))
     ulp = np.abs(got - ref) / np.spacing(np.float32(ref).astype(np.float32)).astype(np.float64)
     assert ulp.max() <= 1.0, ulp.max()
-    assert oracle.exp2f(-126.5) == 0.0 and oracle.exp2f(float("nan")) == 0.0
+    # below the range (and NaN) the argument is raised to -126
+    tiny = np.float32(2.0 ** -126)
+    assert oracle.exp2f(-126.5) == tiny and oracle.exp2f(-1e30) == tiny and oracle.exp2f(float("nan")) == tiny
     # integers are exact
     assert all(oracle.exp2f(float(-k)) == np.float32(2.0 ** -k) for k in range(0, 126))
 
