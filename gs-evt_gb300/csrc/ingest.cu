@@ -94,7 +94,8 @@ extern "C" int gsevt_parse_events_txt(const char *text, size_t len, int64_t *ts,
     // lines in the buffer (a last line without a newline counts too): the output capacity
     // that every chunk's placement at its first line's index needs
     size_t lines = 0;
-    for (const char *p = text, *e = text + len; (p = (const char *)std::memchr(p, '\n', (size_t)(e - p))); ++p)
+    for (const char *p = text, *e = text + len; (p = (const char *)std::memchr(p, '\n', (size_t)(e - p))) != nullptr;
+         ++p)
         ++lines;
     if (text[len - 1] != '\n') ++lines;
     if (capacity < lines || !ts || !x || !y || !polarity) return GSEVT_ERR_TOO_LARGE;
@@ -120,7 +121,7 @@ extern "C" int gsevt_parse_events_txt(const char *text, size_t len, int64_t *ts,
     auto count_lines = [&](int i) {
         size_t n = 0;
         for (const char *p = ch[(size_t)i].begin, *e = ch[(size_t)i].end;
-             p < e && (p = (const char *)std::memchr(p, '\n', (size_t)(e - p))); ++p)
+             p < e && (p = (const char *)std::memchr(p, '\n', (size_t)(e - p))) != nullptr; ++p)
             ++n;
         nlines[(size_t)i] = n;
     };
