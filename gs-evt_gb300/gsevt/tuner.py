@@ -91,7 +91,10 @@ def tune(bt, space=SPACE, iters=20, passes=2, flush=None, log=None):
     """Coordinate descent over `space` from the defaults; returns (best choice, best ms,
     every timing as a list of (choice, ms))."""
     best = dict(DEFAULTS)
-    best_ms = time_choice(bt, best, iters, flush=flush)
+    # the first timing of a tracker also pays for its first capture and the clock ramp:
+    # the defaults are timed twice and the faster time is the baseline
+    first = time_choice(bt, best, iters, flush=flush)
+    best_ms = min(first, time_choice(bt, best, iters, flush=flush))
     trials = [(dict(best), best_ms)]
     for _ in range(passes):
         changed = False
