@@ -34,7 +34,7 @@ def _worker(rank, world, port, out):
 
 def test_two_gloo_ranks_take_the_slowest_time():
     world = 2
-    with mp.Manager() as man:
+    with mp.get_context("spawn").Manager() as man:  # no fork of a threaded process
         out = man.dict()
         mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
         res = dict(out)
