@@ -42,16 +42,50 @@
 #define GS_KHALF (-0x1.715476p-1f)  // -log2(e) / 2, rounded to FP32
 #define GS_KFULL (-0x1.715476p+0f)  // -log2(e)
 
+__host__ __device__ __forceinline__ uint32_t gs_float_bits(float x)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(x);
+#else
+    union { float f; uint32_t u; } cv;
+    cv.f = x;
+    return cv.u;
+#endif
+}
+
+__host__ __device__ __forceinline__ float gs_bits_float(uint32_t u)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    union { uint32_t u; float f; } cv;
+    cv.u = u;
+    return cv.f;
+#endif
+}
+
 // Deterministic 2^y for y <= 0: k = rint(y), r = y - k (exact, |r| <= 1/2), 2^r = 1 + r c(r)
 // with c a degree-5 near-minimax polynomial (Lawson fit, oracle/fit_exp.py fit_exp2;
 // Horner with fused multiply-adds) and an exact power-of-two scale: below one ulp of 2^y.
-// Bit-identical to or_exp2f in the CPU oracle.  y below -126 (and NaN) is raised to -126:
-// a weight of 2^-126 fails the blends' alpha test exactly as 0 would, one instruction
-// cheaper than a branch.
+// The same value as or_exp2f in the CPU oracle for every float (which states it with
+// rintf and a multiply by 2^k).  y below -126 (and NaN) is raised to -126: a weight of
+// 2^-126 fails the blends' alpha test exactly as 0 would, one instruction cheaper than a
+// branch.
+//
+// No conversion instruction (they issue at a fraction of the FP32 rate, and the blends
+// evaluate this once per pixel and candidate): t = y + 1.5 2^23 lies in [2^23, 2^24),
+// where the float spacing is 1, so the addition rounds y to the nearest integer, ties to
+// even, exactly as rint; k = t - 1.5 2^23 is exact, and the low bits of t hold k in two's
+// complement: bits(t) = bits(1.5 2^23) + k, whence bits(t) << 23 = k << 23 (mod 2^32;
+// bits(1.5 2^23) has no set bit below bit 22).  The scale by 2^k is then an addition to
+// the exponent field of p, which equals the product p 2^k while that product is normal:
+// for y >= -126, k = -126 only with r >= 0, where p >= 1.  (For y > 0 the result is
+// unspecified; every caller discards the weight of a positive exponent.)
 __host__ __device__ __forceinline__ float gs_exp2f(float y)
 {
     y = fmaxf(y, -126.0f);
-    const float k = rintf(y);
+    const float t = y + 0x1.8p23f;
+    const float k = t - 0x1.8p23f;
     const float r = y - k;
     float p = 0x1.41fbb8p-13f;
     p = fmaf(p, r, 0x1.5f3e56p-10f);
@@ -60,15 +94,7 @@ __host__ __device__ __forceinline__ float gs_exp2f(float y)
     p = fmaf(p, r, 0x1.ebfbdcp-3f);
     p = fmaf(p, r, 0x1.62e43p-1f);
     p = fmaf(p, r, 1.0f);
-    const int ki = (int)k;
-#ifdef __CUDA_ARCH__
-    const float sc = __int_as_float((ki + 127) << 23);
-#else
-    union { uint32_t u; float f; } cv;
-    cv.u = (uint32_t)(ki + 127) << 23;
-    const float sc = cv.f;
-#endif
-    return p * sc;
+    return gs_bits_float(gs_float_bits(p) + (gs_float_bits(t) << 23));
 }
 
 // The base-2 exponent coefficients of a record's conic {cx, cy, cz, opacity} (opacity kept).

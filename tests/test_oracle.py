@@ -32,6 +32,57 @@ def test_exp2f_error_bound():
     assert all(oracle.exp2f(float(-k)) == np.float32(2.0 ** -k) for k in range(0, 126))
 
 
+_EXP2_PROBE = r"""
+#include <omp.h>
+#include "common.cuh"
+extern "C" long long exp2_mismatches(float (*ref)(float), unsigned long long lo, unsigned long long hi)
+{
+    long long bad = 0;
+#pragma omp parallel for reduction(+ : bad) schedule(static, 1 << 16)
+    for (long long b = (long long)lo; b <= (long long)hi; ++b) {
+        const float y = gs_bits_float((uint32_t)b);
+        bad += gs_float_bits(gs_exp2f(y)) != gs_float_bits(ref(y));
+    }
+    return bad;
+}
+extern "C" float exp2_one(float y) { return gs_exp2f(y); }
+"""
+
+
+def test_kernel_exp2f_equals_the_oracle_on_every_float(tmp_path):
+    """The kernels' 2^y (gs_exp2f in csrc/common.cuh: rint(y) by the 1.5 2^23 addition and
+    the scale as an exponent-field addition) against the oracle's or_exp2f (rintf and a
+    multiply by 2^k) on every float in [-126, 0] and on the clamped arguments below it.
+    The same source is compiled for the host here; the blend parity tests on the GPU then
+    tie the device instance to the oracle's images bit for bit."""
+    import ctypes
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src, so = tmp_path / "exp2_probe.cu", tmp_path / "exp2_probe.so"
+    src.write_text(_EXP2_PROBE)
+    cmd = [nvcc, "-shared", "-O2", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-fopenmp",
+           "-gencode", "arch=compute_103a,code=sm_103a",
+           "-I", os.path.join(root, "include"), "-I", os.path.join(root, "gs-evt_gb300", "csrc"),
+           str(src), "-o", str(so), "-lgomp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    probe = ctypes.CDLL(str(so))
+    probe.exp2_mismatches.restype = ctypes.c_longlong
+    probe.exp2_mismatches.argtypes = [ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_ulonglong]
+    probe.exp2_one.restype = ctypes.c_float
+    probe.exp2_one.argtypes = [ctypes.c_float]
+    ref = ctypes.cast(oracle.lib().or_exp2f_export, ctypes.c_void_p)
+    # -0.0 (0x80000000) up to -126.0 (0xC2FC0000): every float of the blends' range
+    assert probe.exp2_mismatches(ref, 0x80000000, 0xC2FC0000) == 0
+    assert probe.exp2_mismatches(ref, 0x00000000, 0x00000000) == 0  # +0.0
+    for y in (-126.00001, -126.5, -127.0, -1e30, float("-inf"), float("nan")):
+        assert probe.exp2_one(y) == np.float32(2.0 ** -126) == oracle.exp2f(y)
+
+
 # ------------------------------------------------------------- pose golden --
 @pytest.mark.parametrize("mod", [opose, "product"])
 def test_pose_algebra_golden(mod):
