@@ -43,7 +43,9 @@
  * with c of degree 5 (Lawson's reweighted least squares, oracle/fit_exp.py fit_exp2)
  * evaluated with fused multiply-adds, and an exact power-of-two scale.  Max error below one
  * ulp (checked against numpy in tests/test_oracle.py).  y below -126 and NaN are raised to
- * -126 (2^-126 fails the alpha test as 0 would). */
+ * -126 (2^-126 fails the alpha test as 0 would).  The kernels' gs_exp2f forms rint(y) and
+ * the scale without conversion instructions; tests/test_oracle.py checks that it returns
+ * this function's value for every float in [-126, 0]. */
 #define OR_KHALF (-0x1.715476p-1f)
 #define OR_KFULL (-0x1.715476p+0f)
 static float or_exp2f(float y)
